@@ -1,0 +1,169 @@
+/*
+ * wfs.h — C ABI of the GB300-native wave-function propagation engine.
+ *
+ * Plain C: pointers, sizes and status codes only. One handle owns one grid
+ * (psi, the complex64 potential, phase tables and scratch) on one CUDA
+ * device and one stream. Handles are not thread-safe; use one per host
+ * thread. Every entry point returns 0 (WFS_OK) or a WFS_ERR_* code; the
+ * message is read with wfs_last_error(h) (or wfs_global_error() when no
+ * handle exists yet).
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the WaveFunctionSimPython project root). The reference has no
+ * native FFI; its Python call surface (SimState, operators,
+ * MeasurementTools, core_sim) binds these through ctypes.
+ */
+#ifndef WFS_H
+#define WFS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WFS_ABI_VERSION 1
+
+typedef struct wfs_handle wfs_handle;
+
+enum wfs_status {
+    WFS_OK = 0,
+    WFS_ERR_ARG = 1,          /* invalid argument (shape, size, null pointer) */
+    WFS_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    WFS_ERR_TIMEOUT = 3,      /* a bounded device-side wait gave up */
+    WFS_ERR_NONFINITE = 4,    /* NaN/Inf or norm blow-up detected in psi */
+    WFS_ERR_UNSUPPORTED = 5,  /* axis length or configuration not supported */
+    WFS_ERR_STATE = 6         /* call made in a state that does not allow it */
+};
+
+enum wfs_dtype { WFS_C64 = 0, WFS_C128 = 1 };
+
+/* Element types accepted by wfs_potential_add_raw
+ * (sources/potential.py:26-39: float32, float64, complex64, complex128). */
+enum wfs_raw_type { WFS_RAW_F32 = 0, WFS_RAW_F64 = 1, WFS_RAW_C64 = 2, WFS_RAW_C128 = 3 };
+
+/* Grid description. Replaces the volume/precision part of SimState.__init__
+ * (sources/sim_state.py:83-94): number_of_voxels_3, simulated_volume_dimensions_bohr_radii_3,
+ * double_precision_calculation. psi is C-ordered [x][y][z]. */
+typedef struct {
+    int32_t n[3];       /* voxels per axis; each a product of 2s and 3s, 2..1024 */
+    double extent[3];   /* simulated volume in Bohr radii (delta_x = extent / n) */
+    int32_t dtype;      /* WFS_C64 or WFS_C128 */
+    int32_t device;     /* CUDA device ordinal */
+    void* stream;       /* cudaStream_t to launch on, or NULL for an engine-owned stream */
+} wfs_grid_desc;
+
+/* One potential wall: sources/potential.py:161-198 (PotentialWall). */
+typedef struct {
+    double potential_hartree;
+    double center[3];
+    double normal[3];             /* need not be normalised */
+    double plateau_thickness;
+    double slope_thickness;
+    double slope_exponent;
+    int32_t slit_count;           /* 0..4 */
+    double slit_spacing;
+    double slit_width;
+    double slit_rotation;         /* radians */
+} wfs_wall;
+
+/* Absorbing boundary: sources/potential.py:57-106 (AbsorbingBoundaryCondition). */
+typedef struct {
+    double bottom[3];             /* inner box corners in Bohr radii */
+    double top[3];
+    double offset;                /* start_offset */
+    double potential_pos[3];      /* outer_potential_in_positive_xyz_direction_hartree_3 */
+    double potential_neg[3];
+    double exponent_pos[3];       /* slope_exponent_in_positive_xyz_direction_3 */
+    double exponent_neg[3];
+} wfs_absorbing;
+
+/* Simpson sample box in voxels: first voxel and (odd) sample count per axis.
+ * Built the way sources/measurement.py:101-116 and :320-329 build it. */
+typedef struct {
+    int32_t bottom[3];
+    int32_t count[3];
+} wfs_box;
+
+int wfs_abi_version(void);
+const char* wfs_global_error(void);
+
+/* SimState(config) allocation of psi and V (sources/sim_state.py:63-183, :222-227). */
+int wfs_create(const wfs_grid_desc* desc, wfs_handle** out);
+int wfs_destroy(wfs_handle* h);
+const char* wfs_last_error(const wfs_handle* h);
+int wfs_synchronize(wfs_handle* h);
+
+/* Potential construction (sources/sim_state.py:210-255). */
+int wfs_potential_clear(wfs_handle* h);                                   /* V.fill(0): sources/potential.py:510 */
+int wfs_potential_add_wall(wfs_handle* h, const wfs_wall* w);              /* PotentialWall.add_potential: sources/potential.py:201-242 */
+int wfs_potential_add_absorbing(wfs_handle* h, const wfs_absorbing* a);    /* AbsorbingBoundaryCondition.add_potential: sources/potential.py:108-158 */
+int wfs_potential_add_raw(wfs_handle* h, const void* data, int32_t raw_type, int32_t on_device); /* PreInitializedPotential.add_potential: sources/potential.py:47-55 */
+int wfs_set_potential(wfs_handle* h, const void* v_c64, int32_t on_device);
+int wfs_get_potential(wfs_handle* h, void* v_c64, int32_t to_device);
+
+/* Wave function (sources/sim_state.py:185-208, :309-313; sources/wave_packet.py:217-271). */
+int wfs_init_gaussian(wfs_handle* h, const double sigma[3], const double r0[3], const double k0[3]);
+int wfs_set_psi(wfs_handle* h, const void* psi, int32_t on_device);
+int wfs_get_psi(wfs_handle* h, void* psi, int32_t to_device);
+/* Device pointer of psi in real space (materialises any pending split-step
+ * state first). Valid until the next propagation call. */
+int wfs_psi_device_ptr(wfs_handle* h, void** ptr);
+
+/* Propagators: SimState.evolve_state (sources/sim_state.py:754-762). */
+/* nsteps Strang steps: SimState._fft_time_evolution (sources/sim_state.py:641-697). */
+int wfs_step_split(wfs_handle* h, int32_t nsteps, double dt, double mass);
+/* nsteps power-series steps: SimState._power_series_time_evolution (sources/sim_state.py:721-752).
+ * stencil_order 2 reproduces power_series_operator.cu:50-58; 4 is the 4th-order Laplacian. */
+int wfs_step_taylor(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t order, int32_t stencil_order);
+
+/* Operators module (sources/operators.py:9-55). */
+/* Writes exp(-i |k|^2 dt fraction / m) (fraction 0.25 = the reference's half step,
+ * kinetic_operator.cu:21-23) into out (psi dtype, N elements). */
+int wfs_kinetic_operator(wfs_handle* h, double dt, double mass, double fraction, void* out, int32_t to_device);
+/* inout *= cexp_i(-dt V) (potential_operator.cu:11-15); inout has psi dtype. */
+int wfs_potential_operator(wfs_handle* h, double dt, void* inout, int32_t on_device);
+
+/* Observables (sources/measurement.py:153-188 VolumeProbability, :354-400 ExpectedLocation).
+ * prob_out[nbox]; loc may be NULL, else r_out[3] = <r>, r2_out[3] = <r^2>. FP64 accumulation. */
+int wfs_observe(wfs_handle* h, const wfs_box* boxes, int32_t nbox, const wfs_box* loc,
+                double* prob_out, double* r_out, double* r2_out);
+
+/* Driver loop fused on the device: core_sim.run_iteration (sources/core_sim.py:26-65)
+ * for the split-step method. Before step i (i = 0, interval, 2*interval, ... < nsteps)
+ * the observables are recorded, as time_step does (sources/core_sim.py:19-24):
+ * prob_series[rec*nbox + b], loc_series[rec*6 + (0..2 = <r>, 3..5 = <r^2>)].
+ * The series arrays hold ceil(nsteps / interval) records. */
+int wfs_run_split(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t interval,
+                  const wfs_box* boxes, int32_t nbox, const wfs_box* loc,
+                  double* prob_series, double* loc_series);
+
+/* FP64 norm sum |psi|^2 dV over the whole grid; WFS_ERR_NONFINITE when psi holds NaN/Inf. */
+int wfs_norm(wfs_handle* h, double* norm_out);
+
+/* Instrumentation (no counterpart in the reference, which only times the host
+ * loop, sources/core_sim.py:43-49). When enabled, every kernel launch of the
+ * engine is bracketed by CUDA events on the engine's stream; wfs_profile_read
+ * synchronises and returns the accumulated device milliseconds and launch
+ * counts per pass kind (WFS_NPASS entries each). */
+enum wfs_pass_kind {
+    WFS_PASS_X_KIN = 0,     /* x pencils: Fx, kinetic factor, Fx^-1 */
+    WFS_PASS_Y = 1,         /* y pencils: Fy or Fy^-1 */
+    WFS_PASS_Z_VPH = 2,     /* z rows: Fz^-1, potential phase, Fz */
+    WFS_PASS_Z = 3,         /* z rows: Fz or Fz^-1 */
+    WFS_PASS_OBSERVE = 4,   /* fused or standalone observation reduction */
+    WFS_PASS_TAYLOR = 5,    /* one power-series term */
+    WFS_PASS_OTHER = 6,     /* reductions, phase tables */
+    WFS_NPASS = 8
+};
+/* on: 0 off, 1 on; a value > 1 also pre-creates that many event pairs. */
+int wfs_profile_enable(wfs_handle* h, int32_t on);
+int wfs_profile_read(wfs_handle* h, double* ms_out, int64_t* count_out, int32_t reset);
+/* Number of kernels the engine has launched since creation. */
+int wfs_launch_count(wfs_handle* h, int64_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WFS_H */

@@ -1,0 +1,312 @@
+"""ctypes binding of the engine's C ABI (``include/wfs.h``).
+
+The library ``_wfs.so`` is built in-tree by ``build_ext.build()``. There is no
+fallback: if the library is missing or cannot be loaded, importing the engine
+raises, so a missing CUDA extension can never be mistaken for a working path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_wfs.so"
+
+WFS_OK = 0
+WFS_ERR_ARG = 1
+WFS_ERR_CUDA = 2
+WFS_ERR_TIMEOUT = 3
+WFS_ERR_NONFINITE = 4
+WFS_ERR_UNSUPPORTED = 5
+WFS_ERR_STATE = 6
+WFS_C64 = 0
+WFS_C128 = 1
+RAW_TYPES = {"float32": 0, "float64": 1, "complex64": 2, "complex128": 3}
+MAX_BOX = 8
+
+# Every entry point include/wfs.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "wfs_abi_version", "wfs_global_error", "wfs_create", "wfs_destroy", "wfs_last_error", "wfs_synchronize",
+    "wfs_potential_clear", "wfs_potential_add_wall", "wfs_potential_add_absorbing", "wfs_potential_add_raw",
+    "wfs_set_potential", "wfs_get_potential", "wfs_init_gaussian", "wfs_set_psi", "wfs_get_psi",
+    "wfs_psi_device_ptr", "wfs_step_split", "wfs_step_taylor", "wfs_kinetic_operator", "wfs_potential_operator",
+    "wfs_observe", "wfs_run_split", "wfs_norm", "wfs_profile_enable", "wfs_profile_read", "wfs_launch_count",
+]
+NPASS = 8
+PASS_NAMES = ["x_kin", "y", "z_vph", "z", "observe", "taylor", "other", "unused"]
+
+
+class WfsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"wfs error {code}: {msg}")
+        self.code = code
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("n", C.c_int32 * 3), ("extent", C.c_double * 3), ("dtype", C.c_int32),
+                ("device", C.c_int32), ("stream", C.c_void_p)]
+
+
+class WallDesc(C.Structure):
+    _fields_ = [("potential_hartree", C.c_double), ("center", C.c_double * 3), ("normal", C.c_double * 3),
+                ("plateau_thickness", C.c_double), ("slope_thickness", C.c_double), ("slope_exponent", C.c_double),
+                ("slit_count", C.c_int32), ("slit_spacing", C.c_double), ("slit_width", C.c_double),
+                ("slit_rotation", C.c_double)]
+
+
+class AbsorbingDesc(C.Structure):
+    _fields_ = [("bottom", C.c_double * 3), ("top", C.c_double * 3), ("offset", C.c_double),
+                ("potential_pos", C.c_double * 3), ("potential_neg", C.c_double * 3),
+                ("exponent_pos", C.c_double * 3), ("exponent_neg", C.c_double * 3)]
+
+
+class Box(C.Structure):
+    _fields_ = [("bottom", C.c_int32 * 3), ("count", C.c_int32 * 3)]
+
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None):
+    """Loads ``_wfs.so`` once and declares argument types. Raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"{p} is missing: build it with wavefunctionsimpython_gb300.build_ext.build()")
+    lib = C.CDLL(str(p))
+    vp, i32, dbl = C.c_void_p, C.c_int32, C.c_double
+    dp = C.POINTER(C.c_double)
+    sig = {
+        "wfs_abi_version": ([], C.c_int),
+        "wfs_global_error": ([], C.c_char_p),
+        "wfs_create": ([C.POINTER(GridDesc), C.POINTER(vp)], C.c_int),
+        "wfs_destroy": ([vp], C.c_int),
+        "wfs_last_error": ([vp], C.c_char_p),
+        "wfs_synchronize": ([vp], C.c_int),
+        "wfs_potential_clear": ([vp], C.c_int),
+        "wfs_potential_add_wall": ([vp, C.POINTER(WallDesc)], C.c_int),
+        "wfs_potential_add_absorbing": ([vp, C.POINTER(AbsorbingDesc)], C.c_int),
+        "wfs_potential_add_raw": ([vp, vp, i32, i32], C.c_int),
+        "wfs_set_potential": ([vp, vp, i32], C.c_int),
+        "wfs_get_potential": ([vp, vp, i32], C.c_int),
+        "wfs_init_gaussian": ([vp, dp, dp, dp], C.c_int),
+        "wfs_set_psi": ([vp, vp, i32], C.c_int),
+        "wfs_get_psi": ([vp, vp, i32], C.c_int),
+        "wfs_psi_device_ptr": ([vp, C.POINTER(vp)], C.c_int),
+        "wfs_step_split": ([vp, i32, dbl, dbl], C.c_int),
+        "wfs_step_taylor": ([vp, i32, dbl, dbl, i32, i32], C.c_int),
+        "wfs_kinetic_operator": ([vp, dbl, dbl, dbl, vp, i32], C.c_int),
+        "wfs_potential_operator": ([vp, dbl, vp, i32], C.c_int),
+        "wfs_observe": ([vp, C.POINTER(Box), i32, C.POINTER(Box), dp, dp, dp], C.c_int),
+        "wfs_run_split": ([vp, i32, dbl, dbl, i32, C.POINTER(Box), i32, C.POINTER(Box), dp, dp], C.c_int),
+        "wfs_norm": ([vp, dp], C.c_int),
+        "wfs_profile_enable": ([vp, i32], C.c_int),
+        "wfs_profile_read": ([vp, dp, C.POINTER(C.c_int64), i32], C.c_int),
+        "wfs_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def _d3(v):
+    return (C.c_double * 3)(*[float(x) for x in v])
+
+
+def make_box(bottom, count) -> Box:
+    b = Box()
+    for i in range(3):
+        b.bottom[i] = int(bottom[i])
+        b.count[i] = int(count[i])
+    return b
+
+
+class Engine:
+    """One engine handle: psi, V and tables of one grid on one CUDA device."""
+
+    def __init__(self, n, extent, double_precision=False, device=0, stream=None):
+        self.lib = load()
+        self.n = tuple(int(x) for x in n)
+        self.extent = tuple(float(x) for x in extent)
+        self.double_precision = bool(double_precision)
+        self.dtype = np.complex128 if double_precision else np.complex64
+        d = GridDesc()
+        for i in range(3):
+            d.n[i] = self.n[i]
+            d.extent[i] = self.extent[i]
+        d.dtype = WFS_C128 if double_precision else WFS_C64
+        d.device = int(device)
+        d.stream = stream
+        h = C.c_void_p()
+        rc = self.lib.wfs_create(C.byref(d), C.byref(h))
+        if rc != WFS_OK:
+            raise WfsError(rc, self.lib.wfs_global_error().decode())
+        self.h = h
+
+    @property
+    def dx(self):
+        return tuple(self.extent[i] / self.n[i] for i in range(3))
+
+    def _ck(self, rc):
+        if rc != WFS_OK:
+            raise WfsError(rc, self.lib.wfs_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wfs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- potential ---
+    def potential_clear(self):
+        self._ck(self.lib.wfs_potential_clear(self.h))
+
+    def add_wall(self, potential_hartree, center, normal, plateau, slope=0.0, slope_exponent=1.0,
+                 slit_count=0, slit_spacing=1.0, slit_width=0.5, slit_rotation=0.0):
+        w = WallDesc(float(potential_hartree), _d3(center), _d3(normal), float(plateau), float(slope),
+                     float(slope_exponent), int(slit_count), float(slit_spacing), float(slit_width),
+                     float(slit_rotation))
+        self._ck(self.lib.wfs_potential_add_wall(self.h, C.byref(w)))
+
+    def add_absorbing(self, bottom, top, offset, potential_pos, potential_neg, exponent_pos, exponent_neg):
+        a = AbsorbingDesc(_d3(bottom), _d3(top), float(offset), _d3(potential_pos), _d3(potential_neg),
+                          _d3(exponent_pos), _d3(exponent_neg))
+        self._ck(self.lib.wfs_potential_add_absorbing(self.h, C.byref(a)))
+
+    def add_raw_potential(self, array: np.ndarray):
+        arr = np.ascontiguousarray(array)
+        if arr.shape != self.n:
+            raise ValueError(f"raw potential shape {arr.shape} != grid {self.n}")
+        t = RAW_TYPES.get(arr.dtype.name)
+        if t is None:
+            raise ValueError(f"unsupported raw potential dtype {arr.dtype}")
+        self._ck(self.lib.wfs_potential_add_raw(self.h, arr.ctypes.data, t, 0))
+
+    def set_potential(self, V: np.ndarray):
+        arr = np.ascontiguousarray(V, dtype=np.complex64)
+        if arr.shape != self.n:
+            raise ValueError("potential shape mismatch")
+        self._ck(self.lib.wfs_set_potential(self.h, arr.ctypes.data, 0))
+
+    def get_potential(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.complex64)
+        self._ck(self.lib.wfs_get_potential(self.h, out.ctypes.data, 0))
+        return out
+
+    # --- psi ---
+    def init_gaussian(self, sigma, r0, k0):
+        self._ck(self.lib.wfs_init_gaussian(self.h, _d3(sigma), _d3(r0), _d3(k0)))
+
+    def set_psi(self, psi):
+        if hasattr(psi, "__cuda_array_interface__"):
+            ci = psi.__cuda_array_interface__
+            if tuple(ci["shape"]) != self.n or np.dtype(ci["typestr"]) != np.dtype(self.dtype):
+                raise ValueError("device psi has the wrong shape or dtype")
+            if ci.get("strides") not in (None,):
+                exp = tuple(np.dtype(self.dtype).itemsize * int(np.prod(self.n[i + 1:])) for i in range(3))
+                if tuple(ci["strides"]) != exp:
+                    raise ValueError("device psi must be C-contiguous")
+            self._ck(self.lib.wfs_set_psi(self.h, C.c_void_p(ci["data"][0]), 1))
+            return
+        arr = np.ascontiguousarray(psi, dtype=self.dtype)
+        if arr.shape != self.n:
+            raise ValueError(f"psi shape {arr.shape} != grid {self.n}")
+        self._ck(self.lib.wfs_set_psi(self.h, arr.ctypes.data, 0))
+
+    def get_psi(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=self.dtype)
+        self._ck(self.lib.wfs_get_psi(self.h, out.ctypes.data, 0))
+        return out
+
+    def psi_device_ptr(self) -> int:
+        p = C.c_void_p()
+        self._ck(self.lib.wfs_psi_device_ptr(self.h, C.byref(p)))
+        return int(p.value or 0)
+
+    # --- propagation ---
+    def step_split(self, nsteps, dt, mass=1.0):
+        self._ck(self.lib.wfs_step_split(self.h, int(nsteps), float(dt), float(mass)))
+
+    def step_taylor(self, nsteps, dt, mass=1.0, order=10, stencil_order=2):
+        self._ck(self.lib.wfs_step_taylor(self.h, int(nsteps), float(dt), float(mass), int(order), int(stencil_order)))
+
+    def kinetic_operator(self, dt, mass=1.0, fraction=0.25) -> np.ndarray:
+        out = np.empty(self.n, dtype=self.dtype)
+        self._ck(self.lib.wfs_kinetic_operator(self.h, float(dt), float(mass), float(fraction), out.ctypes.data, 0))
+        return out
+
+    def potential_operator(self, dt, inout: np.ndarray) -> np.ndarray:
+        arr = np.ascontiguousarray(inout, dtype=self.dtype).copy()
+        self._ck(self.lib.wfs_potential_operator(self.h, float(dt), arr.ctypes.data, 0))
+        return arr
+
+    def synchronize(self):
+        self._ck(self.lib.wfs_synchronize(self.h))
+
+    # --- observables ---
+    @staticmethod
+    def _boxes(boxes):
+        nb = len(boxes)
+        if nb > MAX_BOX:
+            raise ValueError(f"at most {MAX_BOX} volume boxes per observation")
+        arr = (Box * max(nb, 1))()
+        for i, (b, c) in enumerate(boxes):
+            arr[i] = make_box(b, c)
+        return arr, nb
+
+    def observe(self, boxes=(), loc=None):
+        """boxes: [(bottom_voxel, count)], loc: (bottom_voxel, count) or None.
+        Returns (probabilities[nbox], <r>[3] or None, <r^2>[3] or None)."""
+        arr, nb = self._boxes(boxes)
+        lb = make_box(*loc) if loc is not None else None
+        prob = (C.c_double * max(nb, 1))()
+        r = (C.c_double * 3)()
+        r2 = (C.c_double * 3)()
+        self._ck(self.lib.wfs_observe(self.h, arr, nb, C.byref(lb) if lb is not None else None, prob, r, r2))
+        return (np.array(prob[:nb]), np.array(r[:]) if lb is not None else None,
+                np.array(r2[:]) if lb is not None else None)
+
+    def run_split(self, nsteps, dt, mass=1.0, interval=1, boxes=(), loc=None):
+        arr, nb = self._boxes(boxes)
+        lb = make_box(*loc) if loc is not None else None
+        nrec = -(-int(nsteps) // int(interval)) if (nb or lb is not None) else 0
+        ps = np.zeros((max(nrec, 1), max(nb, 1)), dtype=np.float64)
+        ls = np.zeros((max(nrec, 1), 6), dtype=np.float64)
+        self._ck(self.lib.wfs_run_split(self.h, int(nsteps), float(dt), float(mass), int(interval), arr, nb,
+                                        C.byref(lb) if lb is not None else None,
+                                        ps.ctypes.data_as(C.POINTER(C.c_double)),
+                                        ls.ctypes.data_as(C.POINTER(C.c_double))))
+        return ps[:nrec, :nb], ls[:nrec]
+
+    def profile_enable(self, on=True, capacity=0):
+        v = (max(int(capacity), 1) if capacity else 1) if on else 0
+        self._ck(self.lib.wfs_profile_enable(self.h, v))
+
+    def profile_read(self, reset=True):
+        """Returns {pass name: (total ms, launches)} accumulated since the last reset."""
+        ms = (C.c_double * NPASS)()
+        cnt = (C.c_int64 * NPASS)()
+        self._ck(self.lib.wfs_profile_read(self.h, ms, cnt, 1 if reset else 0))
+        return {PASS_NAMES[k]: (ms[k], cnt[k]) for k in range(NPASS) if cnt[k]}
+
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        self._ck(self.lib.wfs_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    def norm(self) -> float:
+        v = C.c_double()
+        self._ck(self.lib.wfs_norm(self.h, C.byref(v)))
+        return v.value

@@ -1,0 +1,937 @@
+// engine.cu — host side of the C ABI declared in include/wfs.h.
+//
+// Split-operator schedule. The reference step (sources/sim_state.py:641-697)
+// is S = P V P with P = F^-1 K/2 F. With F = Fx Fy Fz applied as one pencil
+// pass per axis and the kinetic factor K = Kx Ky Kz separable, the engine
+// keeps psi in one of four representations and applies S as
+//   X[Fx K Fx^-1]  Y[Fy^-1]  Z[Fz^-1 E Fz]  Y[Fy]      (E = exp(-i dt V))
+// per step, merging the trailing K/2 of one step with the leading K/2 of the
+// next (Strang merging). Representations of the stored array:
+//   REAL    psi_n                      (x, y, z)
+//   G       Fz psi_n                   (x, y, kz)
+//   H       Fy Fz psi_n                (x, ky, kz)
+//   PENDING Fy Fz V P psi_{n-1}; psi_n = X[Fx K/2 Fx^-1] of it, in H form.
+// Reading psi or observing materialises what is needed; observation from
+// PENDING costs X[K/2] + Y[Fy^-1] + a read-only Z[Fz^-1 observe] pass.
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/wfs.h"
+#include "kernels.h"
+
+using namespace wfs;
+
+namespace {
+
+thread_local std::string g_error;
+
+enum Rep { REP_REAL = 0, REP_G = 1, REP_H = 2, REP_PENDING = 3 };
+
+struct KinTables {
+    double dt = std::nan(""), mass = std::nan(""), frac = std::nan("");
+    void* k[3] = {nullptr, nullptr, nullptr};
+};
+
+}  // namespace
+
+struct wfs_handle {
+    int n[3];
+    double extent[3];
+    double dx[3];
+    int dtype;
+    int device;
+    cudaStream_t stream;
+    bool own_stream;
+    int64_t count;
+    size_t elem;          // bytes per psi element
+    void* psi;            // live psi buffer
+    void* scratch[2];     // Taylor buffers (allocated on first use)
+    float2* V;
+    void* ephase;         // exp(-i dt V) in psi precision
+    double ephase_dt;
+    bool ephase_valid;
+    void* tw[3];          // twiddle tables per axis
+    KinTables kin_half, kin_full;
+    Rep rep;
+    double pend_dt, pend_mass;
+    double* partials;     // observation scratch, per-CTA FP64 sums
+    size_t partials_cap;  // doubles
+    double* series;       // device observation series of wfs_run_split
+    size_t series_cap;    // doubles
+    double* dres;         // device results
+    double* hres;         // pinned host results
+    int* dflag;
+    std::string err;
+    // per-pass CUDA-event profile (wfs_profile_enable / wfs_profile_read)
+    bool prof_on;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_live;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_pool;
+    double prof_ms[WFS_NPASS];
+    int64_t prof_count[WFS_NPASS];
+    int64_t launches;
+};
+
+namespace {
+
+int set_err(wfs_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    g_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return set_err(h, WFS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+bool is_dbl(const wfs_handle* h) { return h->dtype == WFS_C128; }
+
+// Brackets one kernel launch with CUDA events when profiling is on and counts launches.
+struct PassScope {
+    wfs_handle* h;
+    int kind;
+    cudaEvent_t e1 = nullptr, e2 = nullptr;
+    PassScope(wfs_handle* hh, int k) : h(hh), kind(k) {
+        h->launches += 1;
+        if (!h->prof_on) return;
+        if (h->prof_pool.empty()) {
+            cudaEvent_t a, b;
+            if (cudaEventCreate(&a) != cudaSuccess) return;
+            if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return; }
+            h->prof_pool.push_back({a, b});
+        }
+        e1 = h->prof_pool.back().first;
+        e2 = h->prof_pool.back().second;
+        h->prof_pool.pop_back();
+        cudaEventRecord(e1, h->stream);
+    }
+    ~PassScope() {
+        if (!e1) return;
+        cudaEventRecord(e2, h->stream);
+        h->prof_live.push_back({kind, {e1, e2}});
+    }
+};
+
+int ensure_partials(wfs_handle* h, size_t need) {
+    if (need <= h->partials_cap) return WFS_OK;
+    if (h->partials) cudaFree(h->partials);
+    h->partials = nullptr;
+    h->partials_cap = 0;
+    CK(cudaMalloc(&h->partials, need * sizeof(double)));
+    h->partials_cap = need;
+    return WFS_OK;
+}
+
+template <typename R>
+int upload_roots(wfs_handle* h, int axis) {
+    const int L = h->n[axis];
+    std::vector<Cx<R>> t(L);
+    for (int m = 0; m < L; ++m) {
+        const double a = -2.0 * M_PI * double(m) / double(L);
+        t[m] = mk<R>(R(std::cos(a)), R(std::sin(a)));
+    }
+    CK(cudaMalloc(&h->tw[axis], L * sizeof(Cx<R>)));
+    CK(cudaMemcpy(h->tw[axis], t.data(), L * sizeof(Cx<R>), cudaMemcpyHostToDevice));
+    return WFS_OK;
+}
+
+// Per-axis kinetic factors exp(-i k^2 dt frac / m), k = 2 pi fftfreq(N, dx)
+// (sources/sim_state.py:275-278, kinetic_operator.cu:20-23).
+template <typename R>
+int ensure_kin(wfs_handle* h, KinTables& kt, double dt, double mass, double frac) {
+    if (kt.dt == dt && kt.mass == mass && kt.frac == frac && kt.k[0]) return WFS_OK;
+    for (int a = 0; a < 3; ++a) {
+        const int L = h->n[a];
+        std::vector<Cx<R>> v(L);
+        for (int i = 0; i < L; ++i) {
+            const int fi = (i < (L + 1) / 2) ? i : i - L;  // fftfreq ordering
+            const double k = 2.0 * M_PI * double(fi) / (double(L) * h->dx[a]);
+            const double ang = -k * k * dt * frac / mass;
+            v[i] = mk<R>(R(std::cos(ang)), R(std::sin(ang)));
+        }
+        if (!kt.k[a]) CK(cudaMalloc(&kt.k[a], L * sizeof(Cx<R>)));
+        CK(cudaMemcpy(kt.k[a], v.data(), L * sizeof(Cx<R>), cudaMemcpyHostToDevice));
+    }
+    kt.dt = dt;
+    kt.mass = mass;
+    kt.frac = frac;
+    return WFS_OK;
+}
+
+template <typename R>
+int ensure_ephase(wfs_handle* h, double dt) {
+    if (h->ephase_valid && h->ephase_dt == dt) return WFS_OK;
+    if (!h->ephase) CK(cudaMalloc(&h->ephase, h->count * sizeof(Cx<R>)));
+    PassScope ps(h, WFS_PASS_OTHER);
+    CK(launch_vphase<R>(reinterpret_cast<Cx<R>*>(h->ephase), h->V, dt, h->count, h->stream));
+    h->ephase_dt = dt;
+    h->ephase_valid = true;
+    return WFS_OK;
+}
+
+// ---- single passes --------------------------------------------------------
+template <typename R>
+PassArgs<R> base_args(wfs_handle* h, int axis) {
+    PassArgs<R> a;
+    std::memset(&a, 0, sizeof(a));
+    a.data = reinterpret_cast<Cx<R>*>(h->psi);
+    a.tw = reinterpret_cast<const Cx<R>*>(h->tw[axis]);
+    a.scale = R(1);
+    return a;
+}
+
+template <typename R>
+int pass_x_kin(wfs_handle* h, KinTables& kt) {
+    PassArgs<R> a = base_args<R>(h, 0);
+    const int64_t plane = int64_t(h->n[1]) * h->n[2];
+    a.outer_stride = 0;
+    a.row_stride = plane;
+    a.ncols = int32_t(plane);
+    a.k_row = reinterpret_cast<const Cx<R>*>(kt.k[0]);
+    a.k_c1 = reinterpret_cast<const Cx<R>*>(kt.k[1]);
+    a.k_c2 = reinterpret_cast<const Cx<R>*>(kt.k[2]);
+    a.c2n = h->n[2];
+    a.scale = R(1.0 / double(h->n[0]));
+    PassScope ps(h, WFS_PASS_X_KIN);
+    CK(launch_fft_strided<R>(h->n[0], OP_KIN, a, 1, h->stream));
+    return WFS_OK;
+}
+
+template <typename R>
+int pass_y(wfs_handle* h, int dir) {
+    PassArgs<R> a = base_args<R>(h, 1);
+    a.outer_stride = int64_t(h->n[1]) * h->n[2];
+    a.row_stride = h->n[2];
+    a.ncols = h->n[2];
+    a.dir = dir;
+    a.scale = R(1.0 / std::sqrt(double(h->n[1])));
+    PassScope ps(h, WFS_PASS_Y);
+    CK(launch_fft_strided<R>(h->n[1], OP_PLAIN, a, h->n[0], h->stream));
+    return WFS_OK;
+}
+
+template <typename R>
+int pass_z(wfs_handle* h, int dir) {
+    PassArgs<R> a = base_args<R>(h, 2);
+    a.nrows = int64_t(h->n[0]) * h->n[1];
+    a.dir = dir;
+    a.scale = R(1.0 / std::sqrt(double(h->n[2])));
+    PassScope ps(h, WFS_PASS_Z);
+    CK(launch_fft_contig<R>(h->n[2], OP_PLAIN, a, h->stream, nullptr));
+    return WFS_OK;
+}
+
+template <typename R>
+int pass_z_vph(wfs_handle* h) {
+    PassArgs<R> a = base_args<R>(h, 2);
+    a.nrows = int64_t(h->n[0]) * h->n[1];
+    a.ephase = reinterpret_cast<const Cx<R>*>(h->ephase);
+    a.scale = R(1.0 / double(h->n[2]));
+    PassScope ps(h, WFS_PASS_Z_VPH);
+    CK(launch_fft_contig<R>(h->n[2], OP_VPH, a, h->stream, nullptr));
+    return WFS_OK;
+}
+
+// ---- representation changes ----------------------------------------------
+template <typename R>
+int finish_pending(wfs_handle* h) {
+    if (h->rep != REP_PENDING) return WFS_OK;
+    int rc = ensure_kin<R>(h, h->kin_half, h->pend_dt, h->pend_mass, 0.25);
+    if (rc) return rc;
+    rc = pass_x_kin<R>(h, h->kin_half);
+    if (rc) return rc;
+    h->rep = REP_H;
+    return WFS_OK;
+}
+
+template <typename R>
+int to_H(wfs_handle* h) {
+    int rc = WFS_OK;
+    if (h->rep == REP_PENDING) return finish_pending<R>(h);
+    if (h->rep == REP_REAL) {
+        if ((rc = pass_z<R>(h, -1))) return rc;
+        h->rep = REP_G;
+    }
+    if (h->rep == REP_G) {
+        if ((rc = pass_y<R>(h, -1))) return rc;
+        h->rep = REP_H;
+    }
+    return WFS_OK;
+}
+
+template <typename R>
+int to_real(wfs_handle* h) {
+    int rc = finish_pending<R>(h);
+    if (rc) return rc;
+    if (h->rep == REP_H) {
+        if ((rc = pass_y<R>(h, +1))) return rc;
+        h->rep = REP_G;
+    }
+    if (h->rep == REP_G) {
+        if ((rc = pass_z<R>(h, +1))) return rc;
+        h->rep = REP_REAL;
+    }
+    return WFS_OK;
+}
+
+bool fft_ready(wfs_handle* h) {
+    for (int a = 0; a < 3; ++a)
+        if (!fft_length_supported(h->n[a], is_dbl(h))) {
+            set_err(h, WFS_ERR_UNSUPPORTED, "split-step: axis length " + std::to_string(h->n[a]) +
+                                                " not supported (2^a * 3^b with b <= 1, 2..1024)");
+            return false;
+        }
+    return true;
+}
+
+template <typename R>
+int split_steps(wfs_handle* h, int nsteps, double dt, double mass) {
+    if (nsteps <= 0) return WFS_OK;
+    if (!fft_ready(h)) return WFS_ERR_UNSUPPORTED;
+    int rc;
+    if (h->rep == REP_PENDING && (h->pend_dt != dt || h->pend_mass != mass)) {
+        if ((rc = finish_pending<R>(h))) return rc;
+    }
+    if ((rc = ensure_ephase<R>(h, dt))) return rc;
+    if ((rc = ensure_kin<R>(h, h->kin_half, dt, mass, 0.25))) return rc;
+    if ((rc = ensure_kin<R>(h, h->kin_full, dt, mass, 0.5))) return rc;
+    bool merged = (h->rep == REP_PENDING);
+    if (!merged && (rc = to_H<R>(h))) return rc;
+    for (int s = 0; s < nsteps; ++s) {
+        if ((rc = pass_x_kin<R>(h, merged ? h->kin_full : h->kin_half))) return rc;
+        if ((rc = pass_y<R>(h, +1))) return rc;
+        if ((rc = pass_z_vph<R>(h))) return rc;
+        if ((rc = pass_y<R>(h, -1))) return rc;
+        merged = true;
+    }
+    h->rep = REP_PENDING;
+    h->pend_dt = dt;
+    h->pend_mass = mass;
+    return WFS_OK;
+}
+
+// ---- observation ----------------------------------------------------------
+int fill_obs(wfs_handle* h, const wfs_box* boxes, int nbox, const wfs_box* loc, ObsArgs& o) {
+    if (nbox < 0 || nbox > kMaxBox) return set_err(h, WFS_ERR_ARG, "nbox must be in [0, 8]");
+    if (nbox > 0 && !boxes) return set_err(h, WFS_ERR_ARG, "boxes is null");
+    std::memset(&o, 0, sizeof(o));
+    o.nbox = nbox;
+    auto cp = [&](const wfs_box& b, ObsBox& d) -> bool {
+        for (int a = 0; a < 3; ++a) {
+            if (b.count[a] < 1 || b.bottom[a] < 0 || b.bottom[a] + b.count[a] > h->n[a]) return false;
+            d.b[a] = b.bottom[a];
+            d.c[a] = b.count[a];
+        }
+        return true;
+    };
+    for (int b = 0; b < nbox; ++b)
+        if (!cp(boxes[b], o.box[b])) return set_err(h, WFS_ERR_ARG, "observation box outside the grid");
+    o.has_loc = loc ? 1 : 0;
+    if (loc && !cp(*loc, o.loc)) return set_err(h, WFS_ERR_ARG, "location box outside the grid");
+    for (int a = 0; a < 3; ++a) {
+        o.n[a] = h->n[a];
+        o.dx[a] = h->dx[a];
+    }
+    o.nq = nbox + (loc ? kLocQ : 0);
+    return WFS_OK;
+}
+
+// Launches the observation reduction for the current psi without changing the
+// represented state; results (raw Simpson sums) land in dres[0..nq).
+template <typename R>
+int observe_launch(wfs_handle* h, ObsArgs& o, double* dout) {
+    int rc = finish_pending<R>(h);
+    if (rc) return rc;
+    if (o.nq == 0) return WFS_OK;
+    if (h->rep == REP_H) {
+        if ((rc = pass_y<R>(h, +1))) return rc;
+        h->rep = REP_G;
+    }
+    int grid = 0;
+    if (h->rep == REP_G) {
+        const int rows = fft_contig_rows_per_cta(h->n[2], is_dbl(h));
+        const int64_t nrows = int64_t(h->n[0]) * h->n[1];
+        const int64_t g = (nrows + rows - 1) / rows;
+        if ((rc = ensure_partials(h, size_t(g) * o.nq))) return rc;
+        o.partials = h->partials;
+        PassArgs<R> a = base_args<R>(h, 2);
+        a.nrows = nrows;
+        a.scale = R(1.0 / std::sqrt(double(h->n[2])));
+        a.obs = o;
+        PassScope ps(h, WFS_PASS_OBSERVE);
+        CK(launch_fft_contig<R>(h->n[2], OP_OBS, a, h->stream, &grid));
+    } else {
+        const int64_t nrows = int64_t(h->n[0]) * h->n[1];
+        const int64_t g = (nrows + 7) / 8;
+        if ((rc = ensure_partials(h, size_t(g) * o.nq))) return rc;
+        o.partials = h->partials;
+        PassScope ps(h, WFS_PASS_OBSERVE);
+        CK(launch_observe_real<R>(reinterpret_cast<const Cx<R>*>(h->psi), o, h->stream, &grid));
+    }
+    PassScope ps(h, WFS_PASS_OTHER);
+    CK(launch_reduce_partials(h->partials, grid, o.nq, dout, h->stream));
+    return WFS_OK;
+}
+
+// Converts raw sums to the reference's quantities.
+void finish_obs(const wfs_handle* h, const ObsArgs& o, const double* raw, double* prob, double* r, double* r2) {
+    const double dv = h->dx[0] * h->dx[1] * h->dx[2] / 27.0;
+    for (int b = 0; b < o.nbox; ++b)
+        if (prob) prob[b] = raw[b] * dv;
+    if (o.has_loc) {
+        const double* l = raw + o.nbox;
+        for (int a = 0; a < 3; ++a) {
+            if (r) r[a] = l[1 + a] * dv;
+            if (r2) r2[a] = l[4 + a] * dv;
+        }
+    }
+}
+
+template <typename R>
+int do_observe(wfs_handle* h, const wfs_box* boxes, int nbox, const wfs_box* loc, double* prob, double* r, double* r2) {
+    ObsArgs o;
+    int rc = fill_obs(h, boxes, nbox, loc, o);
+    if (rc) return rc;
+    if ((rc = observe_launch<R>(h, o, h->dres))) return rc;
+    if (o.nq) {
+        CK(cudaMemcpyAsync(h->hres, h->dres, o.nq * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    finish_obs(h, o, h->hres, prob, r, r2);
+    return WFS_OK;
+}
+
+template <typename R>
+int do_run_split(wfs_handle* h, int nsteps, double dt, double mass, int interval, const wfs_box* boxes, int nbox,
+                 const wfs_box* loc, double* prob_series, double* loc_series) {
+    if (interval < 1) return set_err(h, WFS_ERR_ARG, "interval must be >= 1");
+    ObsArgs o;
+    int rc = fill_obs(h, boxes, nbox, loc, o);
+    if (rc) return rc;
+    const int nrec = o.nq ? (nsteps + interval - 1) / interval : 0;
+    const size_t need = size_t(nrec) * o.nq;
+    if (need > h->series_cap) {  // kept across calls so repeated runs allocate nothing
+        if (h->series) cudaFree(h->series);
+        h->series = nullptr;
+        h->series_cap = 0;
+        CK(cudaMalloc(&h->series, need * sizeof(double)));
+        h->series_cap = need;
+    }
+    double* dser = h->series;
+    int rec = 0;
+    for (int i = 0; i < nsteps && rc == WFS_OK; i += interval) {
+        if (o.nq) rc = observe_launch<R>(h, o, dser + size_t(rec++) * o.nq);
+        if (rc == WFS_OK) rc = split_steps<R>(h, (i + interval <= nsteps) ? interval : nsteps - i, dt, mass);
+    }
+    if (rc == WFS_OK && nrec) {
+        std::vector<double> raw(size_t(nrec) * o.nq);
+        cudaError_t e = cudaMemcpyAsync(raw.data(), dser, raw.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = set_err(h, WFS_ERR_CUDA, std::string("series copy: ") + cudaGetErrorString(e));
+        for (int k = 0; k < nrec && rc == WFS_OK; ++k) {
+            double rr[3], rr2[3];
+            finish_obs(h, o, raw.data() + size_t(k) * o.nq, prob_series ? prob_series + size_t(k) * nbox : nullptr, rr, rr2);
+            if (loc && loc_series)
+                for (int a = 0; a < 3; ++a) {
+                    loc_series[k * 6 + a] = rr[a];
+                    loc_series[k * 6 + 3 + a] = rr2[a];
+                }
+        }
+    }
+    return rc;
+}
+
+template <typename R>
+int taylor_steps(wfs_handle* h, int nsteps, double dt, double mass, int order, int stencil) {
+    int rc = to_real<R>(h);
+    if (rc) return rc;
+    for (int i = 0; i < 2; ++i)
+        if (!h->scratch[i]) CK(cudaMalloc(&h->scratch[i], h->count * sizeof(Cx<R>)));
+    TaylorArgs<R> t;
+    std::memset(&t, 0, sizeof(t));
+    for (int a = 0; a < 3; ++a) {
+        t.n[a] = h->n[a];
+        t.c4[a] = R(1.0 / (12.0 * h->dx[a] * h->dx[a]));
+    }
+    t.dxq = R(float(h->dx[0]));
+    t.inv2m = R(1) / R(2) / R(mass);
+    t.V = h->V;
+    for (int s = 0; s < nsteps; ++s) {
+        Cx<R>* psi = reinterpret_cast<Cx<R>*>(h->psi);
+        Cx<R>* A = reinterpret_cast<Cx<R>*>(h->scratch[0]);
+        Cx<R>* B = reinterpret_cast<Cx<R>*>(h->scratch[1]);
+        // buffers: s ping-pongs between A and psi (psi is free after term 1); acc lives in B
+        Cx<R>* sp = psi;
+        Cx<R>* sn = A;
+        for (int n = 1; n <= order; ++n) {
+            t.s_prev = sp;
+            t.s_next = (n == order) ? nullptr : sn;
+            t.acc_in = (n == 1) ? psi : B;
+            t.acc_out = B;
+            t.a = R(dt) / R(n);
+            PassScope ps(h, WFS_PASS_TAYLOR);
+            CK(launch_taylor_term<R>(stencil, t, h->stream));
+            Cx<R>* tmp = sp;
+            sp = sn;
+            sn = tmp;
+        }
+        // new psi = B; old psi and A become scratch
+        h->scratch[1] = h->psi;
+        h->psi = B;
+    }
+    return WFS_OK;
+}
+
+int dispatch_err(wfs_handle* h) { return set_err(h, WFS_ERR_ARG, "null handle"); }
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int wfs_abi_version(void) { return WFS_ABI_VERSION; }
+const char* wfs_global_error(void) { return g_error.c_str(); }
+
+int wfs_create(const wfs_grid_desc* d, wfs_handle** out) {
+    wfs_handle* h = nullptr;
+    if (!d || !out) return set_err(nullptr, WFS_ERR_ARG, "null descriptor or output");
+    *out = nullptr;
+    if (d->dtype != WFS_C64 && d->dtype != WFS_C128) return set_err(nullptr, WFS_ERR_ARG, "dtype must be WFS_C64 or WFS_C128");
+    for (int a = 0; a < 3; ++a) {
+        if (d->n[a] < 1 || d->n[a] > (1 << 16)) return set_err(nullptr, WFS_ERR_ARG, "axis length out of range");
+        if (!(d->extent[a] > 0)) return set_err(nullptr, WFS_ERR_ARG, "extent must be positive");
+    }
+    if (int64_t(d->n[0]) * d->n[1] * d->n[2] > (int64_t(1) << 34)) return set_err(nullptr, WFS_ERR_ARG, "grid too large");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_err(nullptr, WFS_ERR_CUDA, "no CUDA device available");
+    if (d->device < 0 || d->device >= ndev) return set_err(nullptr, WFS_ERR_ARG, "device ordinal out of range");
+    h = new wfs_handle();
+    std::memset(h->tw, 0, sizeof(h->tw));
+    h->scratch[0] = h->scratch[1] = nullptr;
+    h->psi = nullptr;
+    h->V = nullptr;
+    h->ephase = nullptr;
+    h->ephase_valid = false;
+    h->partials = nullptr;
+    h->partials_cap = 0;
+    h->series = nullptr;
+    h->series_cap = 0;
+    h->dres = nullptr;
+    h->hres = nullptr;
+    h->dflag = nullptr;
+    h->rep = REP_REAL;
+    h->prof_on = false;
+    h->launches = 0;
+    for (int k = 0; k < WFS_NPASS; ++k) { h->prof_ms[k] = 0.0; h->prof_count[k] = 0; }
+    h->dtype = d->dtype;
+    h->device = d->device;
+    for (int a = 0; a < 3; ++a) {
+        h->n[a] = d->n[a];
+        h->extent[a] = d->extent[a];
+        h->dx[a] = d->extent[a] / double(d->n[a]);
+    }
+    h->count = int64_t(h->n[0]) * h->n[1] * h->n[2];
+    h->elem = is_dbl(h) ? 16 : 8;
+    auto fail = [&](int rc) {
+        std::string m = h->err;
+        wfs_destroy(h);
+        g_error = m;
+        return rc;
+    };
+    if (cudaSetDevice(h->device) != cudaSuccess) return fail(set_err(h, WFS_ERR_CUDA, "cudaSetDevice failed"));
+    if (d->stream) {
+        h->stream = reinterpret_cast<cudaStream_t>(d->stream);
+        h->own_stream = false;
+    } else {
+        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(set_err(h, WFS_ERR_CUDA, "cudaStreamCreate failed"));
+        h->own_stream = true;
+    }
+    cudaError_t e = cudaMalloc(&h->psi, h->count * h->elem);
+    if (e == cudaSuccess) e = cudaMalloc(&h->V, h->count * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&h->dres, 256 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->hres, 256 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->dflag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->psi, 0, h->count * h->elem, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->V, 0, h->count * sizeof(float2), h->stream);
+    if (e != cudaSuccess) return fail(set_err(h, WFS_ERR_CUDA, std::string("allocation: ") + cudaGetErrorString(e)));
+    int rc = WFS_OK;
+    for (int a = 0; a < 3 && rc == WFS_OK; ++a)
+        if (fft_length_supported(h->n[a], is_dbl(h))) rc = is_dbl(h) ? upload_roots<double>(h, a) : upload_roots<float>(h, a);
+    if (rc) return fail(rc);
+    *out = h;
+    return WFS_OK;
+}
+
+int wfs_destroy(wfs_handle* h) {
+    if (!h) return WFS_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void* bufs[] = {h->psi, h->scratch[0], h->scratch[1], h->V, h->ephase, h->partials, h->series, h->dres, h->dflag,
+                    h->tw[0], h->tw[1], h->tw[2], h->kin_half.k[0], h->kin_half.k[1], h->kin_half.k[2],
+                    h->kin_full.k[0], h->kin_full.k[1], h->kin_full.k[2]};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (h->hres) cudaFreeHost(h->hres);
+    for (auto& pe : h->prof_live) { cudaEventDestroy(pe.second.first); cudaEventDestroy(pe.second.second); }
+    for (auto& pe : h->prof_pool) { cudaEventDestroy(pe.first); cudaEventDestroy(pe.second); }
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return WFS_OK;
+}
+
+const char* wfs_last_error(const wfs_handle* h) { return h ? h->err.c_str() : g_error.c_str(); }
+
+int wfs_synchronize(wfs_handle* h) {
+    if (!h) return dispatch_err(h);
+    CK(cudaStreamSynchronize(h->stream));
+    return WFS_OK;
+}
+
+int wfs_potential_clear(wfs_handle* h) {
+    if (!h) return dispatch_err(h);
+    CK(cudaMemsetAsync(h->V, 0, h->count * sizeof(float2), h->stream));
+    h->ephase_valid = false;
+    return WFS_OK;
+}
+
+int wfs_potential_add_wall(wfs_handle* h, const wfs_wall* w) {
+    if (!h) return dispatch_err(h);
+    if (!w) return set_err(h, WFS_ERR_ARG, "null wall");
+    // frame: potential_wall.cu:39-45 and common.cu:348-369, float32 on the host
+    double nn = std::sqrt(w->normal[0] * w->normal[0] + w->normal[1] * w->normal[1] + w->normal[2] * w->normal[2]);
+    if (!(nn > 0)) return set_err(h, WFS_ERR_ARG, "wall normal has zero length");
+    volatile float n[3] = {float(w->normal[0] / nn), float(w->normal[1] / nn), float(w->normal[2] / nn)};
+    volatile float up[3] = {0.f, 1.f, 0.f};
+    volatile float t0 = n[0] * up[0];
+    volatile float t1 = n[1] * up[1];
+    volatile float t2 = n[2] * up[2];
+    volatile float nd = t0 + t1;
+    nd = nd + t2;
+    if (std::fabs(float(nd)) > 0.99f) { up[0] = 0.f; up[2] = 1.f; }
+    auto mul = [](float a, float b) { volatile float r = a * b; return float(r); };
+    auto add = [](float a, float b) { volatile float r = a + b; return float(r); };
+    auto sub = [](float a, float b) { volatile float r = a - b; return float(r); };
+    float c[3] = {sub(mul(n[1], up[2]), mul(n[2], up[1])), sub(mul(n[2], up[0]), mul(n[0], up[2])),
+                  sub(mul(n[0], up[1]), mul(n[1], up[0]))};
+    float cc = add(add(mul(c[0], c[0]), mul(c[1], c[1])), mul(c[2], c[2]));
+    float ln = float(std::sqrt(double(cc)));
+    if (!(ln > 0)) return set_err(h, WFS_ERR_ARG, "degenerate wall frame");
+    float right[3];
+    for (int i = 0; i < 3; ++i) { volatile float r = c[i] / ln; right[i] = r; }
+    volatile float half = float(w->slit_rotation) / 2.0f;
+    float q0 = float(std::cos(double(half)));
+    float s = float(std::sin(double(half)));
+    float q1 = mul(s, n[0]), q2 = mul(s, n[1]), q3 = mul(s, n[2]);
+    float Q[3][3];
+    Q[0][0] = sub(sub(add(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
+    Q[0][1] = mul(2.f, sub(mul(q1, q2), mul(q0, q3)));
+    Q[0][2] = mul(2.f, add(mul(q1, q3), mul(q0, q2)));
+    Q[1][0] = mul(2.f, add(mul(q2, q1), mul(q0, q3)));
+    Q[1][1] = sub(add(sub(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
+    Q[1][2] = mul(2.f, sub(mul(q2, q3), mul(q0, q1)));
+    Q[2][0] = mul(2.f, sub(mul(q3, q1), mul(q0, q2)));
+    Q[2][1] = mul(2.f, add(mul(q3, q2), mul(q0, q1)));
+    Q[2][2] = add(sub(sub(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
+    float rr[3];
+    for (int i = 0; i < 3; ++i) rr[i] = add(add(mul(Q[i][0], right[0]), mul(Q[i][1], right[1])), mul(Q[i][2], right[2]));
+    WallDev wd;
+    wd.U = float(w->potential_hartree);
+    wd.cx = float(w->center[0]); wd.cy = float(w->center[1]); wd.cz = float(w->center[2]);
+    wd.nx = n[0]; wd.ny = n[1]; wd.nz = n[2];
+    wd.rx = rr[0]; wd.ry = rr[1]; wd.rz = rr[2];
+    wd.plateau = float(w->plateau_thickness);
+    wd.slope = float(w->slope_thickness);
+    wd.slope_exp = float(w->slope_exponent);
+    wd.slit_count = w->slit_count < 0 ? 0 : (w->slit_count > 4 ? 4 : w->slit_count);
+    wd.slit_spacing = float(w->slit_spacing);
+    wd.slit_width = float(w->slit_width);
+    float dx[3] = {float(h->dx[0]), float(h->dx[1]), float(h->dx[2])};
+    CK(launch_wall(h->V, h->n, dx, wd, h->stream));
+    h->ephase_valid = false;
+    return WFS_OK;
+}
+
+int wfs_potential_add_absorbing(wfs_handle* h, const wfs_absorbing* a) {
+    if (!h) return dispatch_err(h);
+    if (!a) return set_err(h, WFS_ERR_ARG, "null absorbing description");
+    AbsorbDev ad;
+    for (int i = 0; i < 3; ++i) {
+        ad.bottom[i] = float(a->bottom[i]);
+        ad.top[i] = float(a->top[i]);
+        ad.pp[i] = float(a->potential_pos[i]);
+        ad.pn[i] = float(a->potential_neg[i]);
+        ad.ep[i] = float(a->exponent_pos[i]);
+        ad.en[i] = float(a->exponent_neg[i]);
+    }
+    ad.offset = float(a->offset);
+    float dx[3] = {float(h->dx[0]), float(h->dx[1]), float(h->dx[2])};
+    CK(launch_absorbing(h->V, h->n, dx, ad, h->stream));
+    h->ephase_valid = false;
+    return WFS_OK;
+}
+
+int wfs_potential_add_raw(wfs_handle* h, const void* data, int32_t raw_type, int32_t on_device) {
+    if (!h) return dispatch_err(h);
+    if (!data) return set_err(h, WFS_ERR_ARG, "null data");
+    static const size_t sz[] = {4, 8, 8, 16};
+    if (raw_type < 0 || raw_type > 3) return set_err(h, WFS_ERR_ARG, "raw_type out of range");
+    const size_t bytes = size_t(h->count) * sz[raw_type];
+    const void* src = data;
+    void* tmp = nullptr;
+    if (!on_device) {
+        CK(cudaMalloc(&tmp, bytes));
+        CK(cudaMemcpyAsync(tmp, data, bytes, cudaMemcpyHostToDevice, h->stream));
+        src = tmp;
+    }
+    cudaError_t e = launch_add_raw(h->V, src, raw_type, h->count, h->stream);
+    if (tmp) {
+        cudaStreamSynchronize(h->stream);
+        cudaFree(tmp);
+    }
+    if (e != cudaSuccess) return set_err(h, WFS_ERR_CUDA, std::string("add_raw: ") + cudaGetErrorString(e));
+    h->ephase_valid = false;
+    return WFS_OK;
+}
+
+int wfs_set_potential(wfs_handle* h, const void* v, int32_t on_device) {
+    if (!h) return dispatch_err(h);
+    if (!v) return set_err(h, WFS_ERR_ARG, "null potential");
+    CK(cudaMemcpyAsync(h->V, v, h->count * sizeof(float2), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    if (!on_device) CK(cudaStreamSynchronize(h->stream));
+    h->ephase_valid = false;
+    return WFS_OK;
+}
+
+int wfs_get_potential(wfs_handle* h, void* v, int32_t to_device) {
+    if (!h) return dispatch_err(h);
+    if (!v) return set_err(h, WFS_ERR_ARG, "null output");
+    CK(cudaMemcpyAsync(v, h->V, h->count * sizeof(float2), to_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return WFS_OK;
+}
+
+int wfs_init_gaussian(wfs_handle* h, const double sigma[3], const double r0[3], const double k0[3]) {
+    if (!h) return dispatch_err(h);
+    if (!sigma || !r0 || !k0) return set_err(h, WFS_ERR_ARG, "null packet parameter");
+    const bool dbl = is_dbl(h);
+    // per-axis envelope and coordinate (common.cu:569-586, gaussian_wave_packet.cu:36-40)
+    int total = h->n[0] + h->n[1] + h->n[2];
+    std::vector<double> gd(total), rd(total);
+    std::vector<float> gf(total), rf(total);
+    int off[3] = {0, h->n[0], h->n[0] + h->n[1]};
+    for (int a = 0; a < 3; ++a) {
+        for (int i = 0; i < h->n[a]; ++i) {
+            const int iv = i - h->n[a] / 2;
+            if (dbl) {
+                const double r = h->dx[a] * double(iv);
+                const double aa = 2.0 * sigma[a];
+                const double norm = std::pow(2.0 / M_PI / aa / aa, 0.25);
+                const double d = r - r0[a];
+                gd[off[a] + i] = norm * std::exp(-d * d / aa / aa);
+                rd[off[a] + i] = r;
+            } else {
+                volatile float r = float(h->dx[a]) * float(iv);
+                const float aa = 2.0f * float(sigma[a]);
+                volatile float q = 2.0f / float(M_PI);
+                q = q / aa;
+                q = q / aa;
+                const float norm = std::pow(float(q), 0.25f);
+                volatile float d = float(r) - float(r0[a]);
+                volatile float ex = -float(d) * float(d);
+                ex = ex / aa;
+                ex = ex / aa;
+                volatile float g = norm * std::exp(float(ex));
+                gf[off[a] + i] = g;
+                rf[off[a] + i] = r;
+            }
+        }
+    }
+    const size_t rb = dbl ? sizeof(double) : sizeof(float);
+    void* dbuf = nullptr;
+    CK(cudaMalloc(&dbuf, 2 * total * rb));
+    CK(cudaMemcpyAsync(dbuf, dbl ? (void*)gd.data() : (void*)gf.data(), total * rb, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync((char*)dbuf + total * rb, dbl ? (void*)rd.data() : (void*)rf.data(), total * rb, cudaMemcpyHostToDevice, h->stream));
+    cudaError_t e;
+    if (dbl) {
+        const double* g = reinterpret_cast<const double*>(dbuf);
+        const double* r = g + total;
+        e = launch_gaussian<double>(reinterpret_cast<Cx<double>*>(h->psi), h->n, g, g + off[1], g + off[2], r, r + off[1], r + off[2],
+                                    k0[0], k0[1], k0[2], h->stream);
+    } else {
+        const float* g = reinterpret_cast<const float*>(dbuf);
+        const float* r = g + total;
+        e = launch_gaussian<float>(reinterpret_cast<Cx<float>*>(h->psi), h->n, g, g + off[1], g + off[2], r, r + off[1], r + off[2],
+                                   float(k0[0]), float(k0[1]), float(k0[2]), h->stream);
+    }
+    cudaStreamSynchronize(h->stream);
+    cudaFree(dbuf);
+    if (e != cudaSuccess) return set_err(h, WFS_ERR_CUDA, std::string("gaussian: ") + cudaGetErrorString(e));
+    h->rep = REP_REAL;
+    return WFS_OK;
+}
+
+int wfs_set_psi(wfs_handle* h, const void* psi, int32_t on_device) {
+    if (!h) return dispatch_err(h);
+    if (!psi) return set_err(h, WFS_ERR_ARG, "null psi");
+    CK(cudaMemcpyAsync(h->psi, psi, h->count * h->elem, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    if (!on_device) CK(cudaStreamSynchronize(h->stream));
+    h->rep = REP_REAL;
+    return WFS_OK;
+}
+
+int wfs_get_psi(wfs_handle* h, void* psi, int32_t to_device) {
+    if (!h) return dispatch_err(h);
+    if (!psi) return set_err(h, WFS_ERR_ARG, "null output");
+    int rc = is_dbl(h) ? to_real<double>(h) : to_real<float>(h);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(psi, h->psi, h->count * h->elem, to_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return WFS_OK;
+}
+
+int wfs_psi_device_ptr(wfs_handle* h, void** ptr) {
+    if (!h) return dispatch_err(h);
+    if (!ptr) return set_err(h, WFS_ERR_ARG, "null output");
+    int rc = is_dbl(h) ? to_real<double>(h) : to_real<float>(h);
+    if (rc) return rc;
+    *ptr = h->psi;
+    return WFS_OK;
+}
+
+int wfs_step_split(wfs_handle* h, int32_t nsteps, double dt, double mass) {
+    if (!h) return dispatch_err(h);
+    if (nsteps < 0 || !(mass > 0) || !std::isfinite(dt)) return set_err(h, WFS_ERR_ARG, "invalid nsteps, dt or mass");
+    return is_dbl(h) ? split_steps<double>(h, nsteps, dt, mass) : split_steps<float>(h, nsteps, dt, mass);
+}
+
+int wfs_step_taylor(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t order, int32_t stencil_order) {
+    if (!h) return dispatch_err(h);
+    if (nsteps < 0 || order < 1 || !(mass > 0) || !std::isfinite(dt)) return set_err(h, WFS_ERR_ARG, "invalid nsteps, order, dt or mass");
+    if (stencil_order != 2 && stencil_order != 4) return set_err(h, WFS_ERR_ARG, "stencil_order must be 2 or 4");
+    return is_dbl(h) ? taylor_steps<double>(h, nsteps, dt, mass, order, stencil_order)
+                     : taylor_steps<float>(h, nsteps, dt, mass, order, stencil_order);
+}
+
+int wfs_kinetic_operator(wfs_handle* h, double dt, double mass, double fraction, void* out, int32_t to_device) {
+    if (!h) return dispatch_err(h);
+    if (!out || !(mass > 0)) return set_err(h, WFS_ERR_ARG, "null output or invalid mass");
+    KinTables kt;
+    int rc;
+    void* dev = out;
+    if (!to_device) CK(cudaMalloc(&dev, h->count * h->elem));
+    if (is_dbl(h)) {
+        rc = ensure_kin<double>(h, kt, dt, mass, fraction);
+        if (!rc) CK(launch_kin_product<double>(reinterpret_cast<Cx<double>*>(dev), (Cx<double>*)kt.k[0], (Cx<double>*)kt.k[1], (Cx<double>*)kt.k[2], h->n, h->stream));
+    } else {
+        rc = ensure_kin<float>(h, kt, dt, mass, fraction);
+        if (!rc) CK(launch_kin_product<float>(reinterpret_cast<Cx<float>*>(dev), (Cx<float>*)kt.k[0], (Cx<float>*)kt.k[1], (Cx<float>*)kt.k[2], h->n, h->stream));
+    }
+    if (!to_device && !rc) CK(cudaMemcpyAsync(out, dev, h->count * h->elem, cudaMemcpyDeviceToHost, h->stream));
+    cudaStreamSynchronize(h->stream);
+    for (int a = 0; a < 3; ++a)
+        if (kt.k[a]) cudaFree(kt.k[a]);
+    if (!to_device) cudaFree(dev);
+    return rc;
+}
+
+int wfs_potential_operator(wfs_handle* h, double dt, void* inout, int32_t on_device) {
+    if (!h) return dispatch_err(h);
+    if (!inout) return set_err(h, WFS_ERR_ARG, "null buffer");
+    int rc = is_dbl(h) ? ensure_ephase<double>(h, dt) : ensure_ephase<float>(h, dt);
+    if (rc) return rc;
+    void* dev = inout;
+    if (!on_device) {
+        CK(cudaMalloc(&dev, h->count * h->elem));
+        CK(cudaMemcpyAsync(dev, inout, h->count * h->elem, cudaMemcpyHostToDevice, h->stream));
+    }
+    cudaError_t e = is_dbl(h) ? launch_mul_inplace<double>((Cx<double>*)dev, (const Cx<double>*)h->ephase, h->count, h->stream)
+                              : launch_mul_inplace<float>((Cx<float>*)dev, (const Cx<float>*)h->ephase, h->count, h->stream);
+    if (e == cudaSuccess && !on_device) e = cudaMemcpyAsync(inout, dev, h->count * h->elem, cudaMemcpyDeviceToHost, h->stream);
+    cudaStreamSynchronize(h->stream);
+    if (!on_device) cudaFree(dev);
+    if (e != cudaSuccess) return set_err(h, WFS_ERR_CUDA, std::string("potential_operator: ") + cudaGetErrorString(e));
+    return WFS_OK;
+}
+
+int wfs_observe(wfs_handle* h, const wfs_box* boxes, int32_t nbox, const wfs_box* loc, double* prob_out, double* r_out, double* r2_out) {
+    if (!h) return dispatch_err(h);
+    return is_dbl(h) ? do_observe<double>(h, boxes, nbox, loc, prob_out, r_out, r2_out)
+                     : do_observe<float>(h, boxes, nbox, loc, prob_out, r_out, r2_out);
+}
+
+int wfs_run_split(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t interval, const wfs_box* boxes, int32_t nbox,
+                  const wfs_box* loc, double* prob_series, double* loc_series) {
+    if (!h) return dispatch_err(h);
+    if (nsteps < 0 || !(mass > 0) || !std::isfinite(dt)) return set_err(h, WFS_ERR_ARG, "invalid nsteps, dt or mass");
+    return is_dbl(h) ? do_run_split<double>(h, nsteps, dt, mass, interval, boxes, nbox, loc, prob_series, loc_series)
+                     : do_run_split<float>(h, nsteps, dt, mass, interval, boxes, nbox, loc, prob_series, loc_series);
+}
+
+int wfs_profile_enable(wfs_handle* h, int32_t on) {
+    if (!h) return dispatch_err(h);
+    h->prof_on = on != 0;
+    // on > 1 is a capacity hint: create that many event pairs now, outside any timed region
+    while (on > 1 && int64_t(h->prof_pool.size()) < on) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        h->prof_pool.push_back({a, b});
+    }
+    return WFS_OK;
+}
+
+int wfs_profile_read(wfs_handle* h, double* ms_out, int64_t* count_out, int32_t reset) {
+    if (!h) return dispatch_err(h);
+    CK(cudaStreamSynchronize(h->stream));
+    for (auto& pe : h->prof_live) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess) {
+            h->prof_ms[pe.first] += ms;
+            h->prof_count[pe.first] += 1;
+        }
+        h->prof_pool.push_back(pe.second);
+    }
+    h->prof_live.clear();
+    for (int k = 0; k < WFS_NPASS; ++k) {
+        if (ms_out) ms_out[k] = h->prof_ms[k];
+        if (count_out) count_out[k] = h->prof_count[k];
+        if (reset) { h->prof_ms[k] = 0.0; h->prof_count[k] = 0; }
+    }
+    return WFS_OK;
+}
+
+int wfs_launch_count(wfs_handle* h, int64_t* out) {
+    if (!h) return dispatch_err(h);
+    if (!out) return set_err(h, WFS_ERR_ARG, "null output");
+    *out = h->launches;
+    return WFS_OK;
+}
+
+int wfs_norm(wfs_handle* h, double* norm_out) {
+    if (!h) return dispatch_err(h);
+    if (!norm_out) return set_err(h, WFS_ERR_ARG, "null output");
+    int rc = is_dbl(h) ? to_real<double>(h) : to_real<float>(h);
+    if (rc) return rc;
+    if ((rc = ensure_partials(h, 152 * 8))) return rc;
+    int nb = 0;
+    CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->stream));
+    if (is_dbl(h)) CK(launch_norm<double>((const Cx<double>*)h->psi, h->count, h->partials, &nb, h->dflag, h->stream));
+    else CK(launch_norm<float>((const Cx<float>*)h->psi, h->count, h->partials, &nb, h->dflag, h->stream));
+    CK(launch_reduce_partials(h->partials, nb, 1, h->dres, h->stream));
+    CK(cudaMemcpyAsync(h->hres, h->dres, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, h->dflag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    *norm_out = h->hres[0] * h->dx[0] * h->dx[1] * h->dx[2];
+    if (flag || !std::isfinite(*norm_out)) return set_err(h, WFS_ERR_NONFINITE, "psi holds NaN or Inf");
+    return WFS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,446 @@
+// field_kernels.cu — construction of psi0 and V, phase tables, observables.
+//
+// The potential builders restate the reference's float32 formulas
+// (sources/cuda_kernels/potential_wall.cu:4-83, absorbing_potential.cu:3-307)
+// with explicitly rounded multiplies and adds (__fmul_rn/__fadd_rn), so that
+// no fused multiply-add changes a rounding and the real-valued geometry is
+// reproducible on any host that evaluates the same float32 expression.
+#include "fft_kernels.cuh"
+
+namespace wfs {
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+
+// ---------------------------------------------------------------------------
+// Potential wall — potential_wall.cu:30-82. The frame (normal, rotated right)
+// is computed once on the host.
+// ---------------------------------------------------------------------------
+__global__ void wall_kernel(float2* __restrict__ V, int nx, int ny, int nz, float dxx, float dxy, float dxz, WallDev w) {
+    const int64_t total = int64_t(nx) * ny * nz;
+    for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total; idx += int64_t(gridDim.x) * blockDim.x) {
+        const int z = int(idx % nz);
+        const int y = int((idx / nz) % ny);
+        const int x = int(idx / (int64_t(ny) * nz));
+        const float rx = fm(dxx, fs(float(x), fm(0.5f, float(nx))));
+        const float ry = fm(dxy, fs(float(y), fm(0.5f, float(ny))));
+        const float rz = fm(dxz, fs(float(z), fm(0.5f, float(nz))));
+        const float ax = fs(rx, w.cx), ay = fs(ry, w.cy), az = fs(rz, w.cz);
+        const float d = fabsf(fa(fa(fm(w.nx, ax), fm(w.ny, ay)), fm(w.nz, az)));
+        const float dR = fabsf(fa(fa(fm(w.rx, ax), fm(w.ry, ay)), fm(w.rz, az)));
+        const float sw = w.slit_width, sp = w.slit_spacing;
+        bool skip = false;
+        switch (w.slit_count) {
+            case 1: skip = dR < fm(sw, 0.5f); break;
+            case 2: skip = dR > fm(fs(sp, sw), 0.5f) && dR < fm(fa(sp, sw), 0.5f); break;
+            case 3:
+                skip = (dR < fm(sw, 0.5f)) || (dR > fs(sp, fm(sw, 0.5f)) && dR < fa(sp, fm(sw, 0.5f)));
+                break;
+            case 4:
+                skip = (dR > fm(fs(sp, sw), 0.5f) && dR < fm(fa(sp, sw), 0.5f)) ||
+                       (dR > fs(fm(sp, 1.5f), fm(sw, 0.5f)) && dR < fa(fm(sp, 1.5f), fm(sw, 0.5f)));
+                break;
+            default: break;
+        }
+        if (skip) continue;
+        const float p2 = fm(w.plateau, 0.5f);
+        if (d <= p2) {
+            V[idx].x = fa(V[idx].x, w.U);
+        } else if (d <= fa(p2, w.slope)) {
+            const float tt = fs(1.0f, __fdiv_rn(fs(d, p2), w.slope));
+            V[idx].x = fa(V[idx].x, fm(w.U, powf(tt, w.slope_exp)));
+        }
+    }
+}
+
+cudaError_t launch_wall(float2* V, const int n[3], const float dx[3], const WallDev& w, cudaStream_t s) {
+    const int64_t total = int64_t(n[0]) * n[1] * n[2];
+    int grid = int((total + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    wall_kernel<<<grid, 256, 0, s>>>(V, n[0], n[1], n[2], dx[0], dx[1], dx[2], w);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Absorbing boundary — absorbing_potential.cu:37-306
+// ---------------------------------------------------------------------------
+struct F3 { float x, y, z; };
+__device__ __forceinline__ F3 f3(float a, float b, float c) { return F3{a, b, c}; }
+// common.cu:394-397
+__device__ __forceinline__ float mixf(F3 v, float u, float w) {
+    return fa(fm(v.z, w), fm(fs(1.0f, w), fa(fm(v.y, u), fm(v.x, fs(1.0f, u)))));
+}
+__device__ __forceinline__ float len3(float a, float b, float c) {
+    return __fsqrt_rn(fa(fa(fm(a, a), fm(b, b)), fm(c, c)));
+}
+__device__ __forceinline__ float ramp(float dist, float off, float maxD, float e, float pot) {
+    return fm(powf(__fdiv_rn(fmaxf(fs(dist, off), 0.0f), maxD), e), pot);
+}
+__device__ __forceinline__ float ang(float num, float den) {  // atan(num/den)/pi*2
+    return fm(__fdiv_rn(atanf(__fdiv_rn(num, den)), 3.14159265358979323846f), 2.0f);
+}
+
+__global__ void absorbing_kernel(float2* __restrict__ V, int nx, int ny, int nz, float dxx, float dxy, float dxz, AbsorbDev a) {
+    const int64_t total = int64_t(nx) * ny * nz;
+    const float off = a.offset;
+    const F3 box_half = f3(fm(fm(0.5f, float(nx)), dxx), fm(fm(0.5f, float(ny)), dxy), fm(fm(0.5f, float(nz)), dxz));
+    const F3 ab = f3(fabsf(a.bottom[0]), fabsf(a.bottom[1]), fabsf(a.bottom[2]));
+    const F3 at = f3(fabsf(a.top[0]), fabsf(a.top[1]), fabsf(a.top[2]));
+    for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total; idx += int64_t(gridDim.x) * blockDim.x) {
+        const int z = int(idx % nz);
+        const int y = int((idx / nz) % ny);
+        const int x = int(idx / (int64_t(ny) * nz));
+        const float rx = fs(fm(dxx, float(x)), fm(fm(0.5f, float(nx)), dxx));
+        const float ry = fs(fm(dxy, float(y)), fm(fm(0.5f, float(ny)), dxy));
+        const float rz = fs(fm(dxz, float(z)), fm(fm(0.5f, float(nz)), dxz));
+        const float Bx = fs(rx, a.bottom[0]), By = fs(ry, a.bottom[1]), Bz = fs(rz, a.bottom[2]);
+        const float Tx = fs(rx, a.top[0]), Ty = fs(ry, a.top[1]), Tz = fs(rz, a.top[2]);
+        float pot = 0.0f;
+        // maxD = box_half - (|corner| + offset), per component
+        auto md = [&](float hx, float hy, float hz, float cx, float cy, float cz, float ox, float oy, float oz) {
+            return f3(fs(hx, fa(cx, ox)), fs(hy, fa(cy, oy)), fs(hz, fa(cz, oz)));
+        };
+        const float h = 0.0f;
+        // corners of the bottom plate
+        if (Bx < 0.f && By < 0.f && Bz < 0.f) {
+            float u = ang(By, Bx), v = ang(-Bz, __fsqrt_rn(fa(fm(Bx, Bx), fm(By, By))));
+            F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, ab.y, ab.z, off, off, off);
+            pot = ramp(len3(Bx, By, Bz), off, mixf(m, u, v), mixf(f3(a.en[0], a.en[1], a.en[2]), u, v), mixf(f3(a.pn[0], a.pn[1], a.pn[2]), u, v));
+        } else if (Bx < 0.f && By < 0.f && Tz > 0.f) {
+            float u = ang(By, Bx), v = ang(Tz, __fsqrt_rn(fa(fm(Bx, Bx), fm(By, By))));
+            F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, ab.y, at.z, off, off, off);
+            pot = ramp(len3(Bx, By, Tz), off, mixf(m, u, v), mixf(f3(a.en[0], a.en[1], a.ep[2]), u, v), mixf(f3(a.pn[0], a.pn[1], a.pp[2]), u, v));
+        } else if (By < 0.f && Tx > 0.f && Tz > 0.f) {
+            float u = ang(-By, Tx), v = ang(Tz, __fsqrt_rn(fa(fm(Tx, Tx), fm(By, By))));
+            F3 m = md(box_half.x, box_half.y, box_half.z, at.x, ab.y, at.z, off, off, off);
+            pot = ramp(len3(Tx, By, Tz), off, mixf(m, u, v), mixf(f3(a.ep[0], a.en[1], a.ep[2]), u, v), mixf(f3(a.pp[0], a.pn[1], a.pp[2]), u, v));
+        } else if (By < 0.f && Bz < 0.f && Tx > 0.f) {
+            float u = ang(-By, Tx), v = ang(-Bz, __fsqrt_rn(fa(fm(Tx, Tx), fm(By, By))));
+            F3 m = md(box_half.x, box_half.y, box_half.z, at.x, ab.y, ab.z, off, off, off);
+            pot = ramp(len3(Tx, By, Bz), off, mixf(m, u, v), mixf(f3(a.ep[0], a.en[1], a.en[2]), u, v), mixf(f3(a.pp[0], a.pn[1], a.pn[2]), u, v));
+        }
+        // corners of the top plate
+        else if (Tx > 0.f && Ty > 0.f && Tz > 0.f) {
+            float u = ang(Ty, Tx), v = ang(Tz, __fsqrt_rn(fa(fm(Tx, Tx), fm(Ty, Ty))));
+            F3 m = md(box_half.x, box_half.y, box_half.z, at.x, at.y, at.z, off, off, off);
+            pot = ramp(len3(Tx, Ty, Tz), off, mixf(m, u, v), mixf(f3(a.ep[0], a.ep[1], a.ep[2]), u, v), mixf(f3(a.pp[0], a.pp[1], a.pp[2]), u, v));
+        } else if (Bz < 0.f && Tx > 0.f && Ty > 0.f) {
+            float u = ang(Ty, Tx), v = ang(-Bz, __fsqrt_rn(fa(fm(Tx, Tx), fm(Ty, Ty))));
+            F3 m = md(box_half.x, box_half.y, box_half.z, at.x, at.y, ab.z, off, off, off);
+            pot = ramp(len3(Tx, Ty, Bz), off, mixf(m, u, v), mixf(f3(a.ep[0], a.ep[1], a.en[2]), u, v), mixf(f3(a.pp[0], a.pp[1], a.pn[2]), u, v));
+        } else if (Bx < 0.f && Bz < 0.f && Ty > 0.f) {
+            float u = ang(Ty, -Bx), v = ang(-Bz, __fsqrt_rn(fa(fm(Bx, Bx), fm(Ty, Ty))));
+            F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, at.y, ab.z, off, off, off);
+            pot = ramp(len3(Bx, Ty, Bz), off, mixf(m, u, v), mixf(f3(a.en[0], a.ep[1], a.en[2]), u, v), mixf(f3(a.pn[0], a.pp[1], a.pn[2]), u, v));
+        } else if (Bx < 0.f && Ty > 0.f && Tz > 0.f) {
+            float u = ang(Ty, -Bx), v = ang(Tz, __fsqrt_rn(fa(fm(Bx, Bx), fm(Ty, Ty))));
+            F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, at.y, at.z, off, off, off);
+            pot = ramp(len3(Bx, Ty, Tz), off, mixf(m, u, v), mixf(f3(a.en[0], a.ep[1], a.ep[2]), u, v), mixf(f3(a.pn[0], a.pp[1], a.pp[2]), u, v));
+        }
+        // bottom edges
+        else if (Bx < 0.f && By < 0.f && Bz > 0.f && Tz < 0.f) {
+            float u = ang(By, Bx);
+            F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, ab.y, h, off, off, h);
+            pot = ramp(len3(Bx, By, h), off, mixf(m, u, 0.f), mixf(f3(a.en[0], a.en[1], h), u, 0.f), mixf(f3(a.pn[0], a.pn[1], h), u, 0.f));
+        } else if (Bx > 0.f && By < 0.f && Tx < 0.f && Tz > 0.f) {
+            float v = ang(Tz, -By);
+            F3 m = md(box_half.x, box_half.y, box_half.z, h, ab.y, at.z, h, off, off);
+            pot = ramp(len3(h, By, Tz), off, mixf(m, 0.f, v), mixf(f3(h, a.en[1], a.ep[2]), 1.f, v), mixf(f3(h, a.pn[1], a.pp[2]), 1.f, v));
+        } else if (By < 0.f && Bz > 0.f && Tx > 0.f && Tz < 0.f) {
+            float u = ang(-By, Tx);
+            F3 m = md(box_half.x, box_half.y, box_half.z, at.x, ab.y, h, off, off, h);
+            pot = ramp(len3(Tx, By, h), off, mixf(m, u, 0.f), mixf(f3(a.ep[0], a.en[1], h), u, 0.f), mixf(f3(a.pp[0], a.pn[1], h), u, 0.f));
+        } else if (Bx > 0.f && By < 0.f && Bz < 0.f && Tx < 0.f) {
+            float v = ang(Bz, By);
+            F3 m = md(box_half.x, box_half.y, box_half.z, h, ab.y, ab.z, h, off, off);
+            pot = ramp(len3(h, By, Bz), off, mixf(m, 0.f, v), mixf(f3(h, a.en[1], a.en[2]), 1.f, v), mixf(f3(h, a.pn[1], a.pn[2]), 1.f, v));
+        }
+        // pillar edges
+        else if (Bx < 0.f && By > 0.f && Bz < 0.f && Ty < 0.f) {
+            float v = ang(Bz, Bx);
+            F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, h, ab.z, off, h, off);
+            pot = ramp(len3(Bx, h, Bz), off, mixf(m, 0.f, v), mixf(f3(a.en[0], h, a.en[2]), 0.f, v), mixf(f3(a.pn[0], h, a.pn[2]), 0.f, v));
+        } else if (Bx < 0.f && By > 0.f && Ty < 0.f && Tz > 0.f) {
+            float v = ang(Tz, -Bx);
+            F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, h, at.z, off, h, off);
+            pot = ramp(len3(Bx, h, Tz), off, mixf(m, 0.f, v), mixf(f3(a.en[0], h, a.ep[2]), 0.f, v), mixf(f3(a.pn[0], h, a.pp[2]), 0.f, v));
+        } else if (By > 0.f && Tx > 0.f && Ty < 0.f && Tz > 0.f) {
+            float v = ang(Tz, Tx);
+            F3 m = md(box_half.x, box_half.y, box_half.z, at.x, h, at.z, off, h, off);
+            pot = ramp(len3(Tx, h, Tz), off, mixf(m, 0.f, v), mixf(f3(a.ep[0], h, a.ep[2]), 0.f, v), mixf(f3(a.pp[0], h, a.pp[2]), 0.f, v));
+        } else if (By > 0.f && Bz < 0.f && Tx > 0.f && Ty < 0.f) {
+            float v = ang(-Bz, Tx);
+            F3 m = md(box_half.x, box_half.y, box_half.z, at.x, h, ab.z, off, h, off);
+            pot = ramp(len3(Tx, h, Bz), off, mixf(m, 0.f, v), mixf(f3(a.ep[0], h, a.en[2]), 0.f, v), mixf(f3(a.pp[0], h, a.pn[2]), 0.f, v));
+        }
+        // top plane edges
+        else if (Bx < 0.f && Bz > 0.f && Ty > 0.f && Tz < 0.f) {
+            float u = ang(Ty, -Bx);
+            F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, at.y, h, off, off, h);
+            pot = ramp(len3(Bx, Ty, h), off, mixf(m, u, 0.f), mixf(f3(a.en[0], a.ep[1], h), u, 0.f), mixf(f3(a.pn[0], a.pp[1], h), u, 0.f));
+        } else if (Bx > 0.f && Tx < 0.f && Ty > 0.f && Tz > 0.f) {
+            float v = ang(Tz, Ty);
+            F3 m = md(box_half.x, box_half.y, box_half.z, h, at.y, at.z, h, off, off);
+            pot = ramp(len3(h, Ty, Tz), off, mixf(m, 1.f, v), mixf(f3(h, a.ep[1], a.ep[2]), 1.f, v), mixf(f3(h, a.pp[1], a.pp[2]), 1.f, v));
+        } else if (Bz > 0.f && Tx > 0.f && Ty > 0.f && Tz < 0.f) {
+            float u = ang(Ty, Tx);
+            F3 m = md(box_half.x, box_half.y, box_half.z, at.x, at.y, h, off, off, h);
+            pot = ramp(len3(Tx, Ty, h), off, mixf(m, u, 0.f), mixf(f3(a.ep[0], a.ep[1], h), u, 0.f), mixf(f3(a.pp[0], a.pp[1], h), u, 0.f));
+        } else if (Bx > 0.f && Bz < 0.f && Tx < 0.f && Ty > 0.f) {
+            float v = ang(-Bz, Ty);
+            F3 m = md(box_half.x, box_half.y, box_half.z, h, at.y, ab.z, h, off, off);
+            pot = ramp(len3(h, Ty, Bz), off, mixf(m, 0.f, v), mixf(f3(h, a.ep[1], a.en[2]), 0.f, v), mixf(f3(h, a.pp[1], a.pn[2]), 0.f, v));
+        }
+        // box sides
+        else if (Bx > 0.f && By < 0.f && Bz > 0.f && Tx < 0.f && Tz < 0.f) {
+            pot = ramp(-By, off, fs(box_half.y, fa(ab.y, off)), a.en[1], a.pn[1]);
+        } else if (Bx > 0.f && By > 0.f && Tx < 0.f && Ty < 0.f && Tz > 0.f) {
+            pot = ramp(Tz, off, fs(box_half.z, fa(at.z, off)), a.ep[2], a.pp[2]);
+        } else if (By > 0.f && Bz > 0.f && Tx > 0.f && Ty < 0.f && Tz < 0.f) {
+            pot = ramp(Tx, off, fs(box_half.x, fa(at.x, off)), a.ep[0], a.pp[0]);
+        } else if (Bx > 0.f && By > 0.f && Bz < 0.f && Tx < 0.f && Ty < 0.f) {
+            pot = ramp(-Bz, off, fs(box_half.z, fa(ab.z, off)), a.en[2], a.pn[2]);
+        } else if (Bx < 0.f && By > 0.f && Bz > 0.f && Ty < 0.f && Tz < 0.f) {
+            pot = ramp(-Bx, off, fs(box_half.x, fa(ab.x, off)), a.en[0], a.pn[0]);
+        } else if (Bx > 0.f && Bz > 0.f && Tx < 0.f && Ty > 0.f && Tz < 0.f) {
+            pot = ramp(Ty, off, fs(box_half.y, fa(at.y, off)), a.ep[1], a.pp[1]);
+        }
+        V[idx].y = fa(V[idx].y, pot);
+    }
+}
+
+cudaError_t launch_absorbing(float2* V, const int n[3], const float dx[3], const AbsorbDev& a, cudaStream_t s) {
+    const int64_t total = int64_t(n[0]) * n[1] * n[2];
+    int grid = int((total + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    absorbing_kernel<<<grid, 256, 0, s>>>(V, n[0], n[1], n[2], dx[0], dx[1], dx[2], a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Raw pre-initialised potential — sources/potential.py:47-55
+// ---------------------------------------------------------------------------
+__global__ void add_raw_kernel(float2* __restrict__ V, const void* __restrict__ src, int type, int64_t count) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        float re = 0.f, im = 0.f;
+        switch (type) {
+            case 0: re = reinterpret_cast<const float*>(src)[i]; break;
+            case 1: re = float(reinterpret_cast<const double*>(src)[i]); break;
+            case 2: { float2 v = reinterpret_cast<const float2*>(src)[i]; re = v.x; im = v.y; } break;
+            default: { double2 v = reinterpret_cast<const double2*>(src)[i]; re = float(v.x); im = float(v.y); } break;
+        }
+        V[i].x += re;
+        V[i].y += im;
+    }
+}
+cudaError_t launch_add_raw(float2* V, const void* src, int raw_type, int64_t count, cudaStream_t s) {
+    int grid = int((count + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    add_raw_kernel<<<grid, 256, 0, s>>>(V, src, raw_type, count);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Gaussian packet — gaussian_wave_packet.cu:27-42, common.cu:569-605.
+// The per-axis envelopes g_d and coordinates r_d are precomputed (they depend
+// on one index only); the product is formed in the reference's order.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R rmul(R a, R b);
+template <> __device__ __forceinline__ float rmul<float>(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ double rmul<double>(double a, double b) { return __dmul_rn(a, b); }
+template <typename R>
+__device__ __forceinline__ R radd(R a, R b);
+template <> __device__ __forceinline__ float radd<float>(float a, float b) { return __fadd_rn(a, b); }
+template <> __device__ __forceinline__ double radd<double>(double a, double b) { return __dadd_rn(a, b); }
+
+__device__ __forceinline__ void sincos_r(float a, float* s, float* c) { sincosf(a, s, c); }
+__device__ __forceinline__ void sincos_r(double a, double* s, double* c) { sincos(a, s, c); }
+__device__ __forceinline__ float exp_r(float a) { return expf(a); }
+__device__ __forceinline__ double exp_r(double a) { return exp(a); }
+
+template <typename R>
+__global__ void gaussian_kernel(Cx<R>* __restrict__ psi, int nx, int ny, int nz, const R* __restrict__ gx,
+                                const R* __restrict__ gy, const R* __restrict__ gz, const R* __restrict__ rx,
+                                const R* __restrict__ ry, const R* __restrict__ rz, R kx, R ky, R kz) {
+    const int64_t total = int64_t(nx) * ny * nz;
+    for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total; idx += int64_t(gridDim.x) * blockDim.x) {
+        const int z = int(idx % nz);
+        const int y = int((idx / nz) % ny);
+        const int x = int(idx / (int64_t(ny) * nz));
+        const R g = rmul(rmul(gx[x], gy[y]), gz[z]);
+        const R ph = radd(radd(rmul(kx, rx[x]), rmul(ky, ry[y])), rmul(kz, rz[z]));
+        R s, c;
+        sincos_r(ph, &s, &c);
+        psi[idx] = mk<R>(rmul(g, c), rmul(g, s));
+    }
+}
+template <typename R>
+cudaError_t launch_gaussian(Cx<R>* psi, const int n[3], const R* gx, const R* gy, const R* gz, const R* rx,
+                            const R* ry, const R* rz, R kx, R ky, R kz, cudaStream_t s) {
+    const int64_t total = int64_t(n[0]) * n[1] * n[2];
+    int grid = int((total + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    gaussian_kernel<R><<<grid, 256, 0, s>>>(psi, n[0], n[1], n[2], gx, gy, gz, rx, ry, rz, kx, ky, kz);
+    return cudaGetLastError();
+}
+template cudaError_t launch_gaussian<float>(Cx<float>*, const int*, const float*, const float*, const float*,
+                                            const float*, const float*, const float*, float, float, float, cudaStream_t);
+template cudaError_t launch_gaussian<double>(Cx<double>*, const int*, const double*, const double*, const double*,
+                                             const double*, const double*, const double*, double, double, double,
+                                             cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Potential phase table e = cexp_i(-dt V) = e^{-i dt ReV} e^{dt ImV}
+// (potential_operator.cu:11-15, common.cu:98-111), in the wave function's precision.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void vphase_kernel(Cx<R>* __restrict__ e, const float2* __restrict__ V, R dt, int64_t count) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        const float2 v = V[i];
+        const R re = -dt * R(v.x);
+        const R im = -dt * R(v.y);
+        R s, c;
+        sincos_r(re, &s, &c);
+        const R m = exp_r(-im);
+        e[i] = mk<R>(c * m, s * m);
+    }
+}
+template <typename R>
+cudaError_t launch_vphase(Cx<R>* e, const float2* V, double dt, int64_t count, cudaStream_t s) {
+    int grid = int((count + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    vphase_kernel<R><<<grid, 256, 0, s>>>(e, V, R(dt), count);
+    return cudaGetLastError();
+}
+template cudaError_t launch_vphase<float>(Cx<float>*, const float2*, double, int64_t, cudaStream_t);
+template cudaError_t launch_vphase<double>(Cx<double>*, const float2*, double, int64_t, cudaStream_t);
+
+// out[x][y][z] = kx[x] * ky[y] * kz[z]  (kinetic operator array for the operators module)
+template <typename R>
+__global__ void kin_product_kernel(Cx<R>* __restrict__ out, const Cx<R>* kx, const Cx<R>* ky, const Cx<R>* kz, int nx, int ny, int nz) {
+    const int64_t total = int64_t(nx) * ny * nz;
+    for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total; idx += int64_t(gridDim.x) * blockDim.x) {
+        const int z = int(idx % nz);
+        const int y = int((idx / nz) % ny);
+        const int x = int(idx / (int64_t(ny) * nz));
+        out[idx] = cmul(cmul(kx[x], ky[y]), kz[z]);
+    }
+}
+template <typename R>
+cudaError_t launch_kin_product(Cx<R>* out, const Cx<R>* kx, const Cx<R>* ky, const Cx<R>* kz, const int n[3], cudaStream_t s) {
+    const int64_t total = int64_t(n[0]) * n[1] * n[2];
+    int grid = int((total + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    kin_product_kernel<R><<<grid, 256, 0, s>>>(out, kx, ky, kz, n[0], n[1], n[2]);
+    return cudaGetLastError();
+}
+template cudaError_t launch_kin_product<float>(Cx<float>*, const Cx<float>*, const Cx<float>*, const Cx<float>*, const int*, cudaStream_t);
+template cudaError_t launch_kin_product<double>(Cx<double>*, const Cx<double>*, const Cx<double>*, const Cx<double>*, const int*, cudaStream_t);
+
+template <typename R>
+__global__ void mul_inplace_kernel(Cx<R>* __restrict__ io, const Cx<R>* __restrict__ f, int64_t count) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
+        io[i] = cmul(io[i], f[i]);
+}
+template <typename R>
+cudaError_t launch_mul_inplace(Cx<R>* inout, const Cx<R>* f, int64_t count, cudaStream_t s) {
+    int grid = int((count + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    mul_inplace_kernel<R><<<grid, 256, 0, s>>>(inout, f, count);
+    return cudaGetLastError();
+}
+template cudaError_t launch_mul_inplace<float>(Cx<float>*, const Cx<float>*, int64_t, cudaStream_t);
+template cudaError_t launch_mul_inplace<double>(Cx<double>*, const Cx<double>*, int64_t, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Observables on real-space psi: one warp per (x, y) row, per-CTA FP64 partials.
+// ---------------------------------------------------------------------------
+constexpr int kObsRowsPerCta = 8;
+
+template <typename R>
+__global__ void __launch_bounds__(256) observe_real_kernel(const Cx<R>* __restrict__ psi, const ObsArgs o) {
+    __shared__ double scratch[(kMaxBox + kLocQ) * 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t nrows = int64_t(o.n[0]) * o.n[1];
+    const int64_t row = int64_t(blockIdx.x) * kObsRowsPerCta + warp;
+    double acc[kMaxBox + kLocQ];
+#pragma unroll
+    for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = 0.0;
+    if (row < nrows) {
+        const int x = int(row / o.n[1]), y = int(row % o.n[1]);
+        R wxy[kMaxBox], lxy, rx, ry;
+        obs_row_factors<R>(o, x, y, wxy, lxy, rx, ry);
+        const Cx<R>* rp = psi + row * o.n[2];
+        for (int z = lane; z < o.n[2]; z += 32) obs_element<R>(o, acc, wxy, lxy, rx, ry, z, rp[z]);
+    }
+    obs_store(o, acc, scratch);
+}
+template <typename R>
+cudaError_t launch_observe_real(const Cx<R>* psi, const ObsArgs& o, cudaStream_t s, int* grid_out) {
+    const int64_t nrows = int64_t(o.n[0]) * o.n[1];
+    const int grid = int((nrows + kObsRowsPerCta - 1) / kObsRowsPerCta);
+    *grid_out = grid;
+    observe_real_kernel<R><<<grid, 32 * kObsRowsPerCta, 0, s>>>(psi, o);
+    return cudaGetLastError();
+}
+template cudaError_t launch_observe_real<float>(const Cx<float>*, const ObsArgs&, cudaStream_t, int*);
+template cudaError_t launch_observe_real<double>(const Cx<double>*, const ObsArgs&, cudaStream_t, int*);
+
+// Deterministic second stage: out[q] = sum over CTAs of partials[cta][q].
+__global__ void reduce_partials_kernel(const double* __restrict__ partials, int nblocks, int nq, double* __restrict__ out) {
+    __shared__ double sh[256];
+    for (int q = 0; q < nq; ++q) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[int64_t(b) * nq + q];
+        sh[threadIdx.x] = s;
+        __syncthreads();
+        for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+            if (threadIdx.x < off) sh[threadIdx.x] += sh[threadIdx.x + off];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[q] = sh[0];
+        __syncthreads();
+    }
+}
+cudaError_t launch_reduce_partials(const double* partials, int nblocks, int nq, double* out, cudaStream_t s) {
+    reduce_partials_kernel<<<1, 256, 0, s>>>(partials, nblocks, nq, out);
+    return cudaGetLastError();
+}
+
+// FP64 norm over the whole grid and a non-finite flag.
+template <typename R>
+__global__ void __launch_bounds__(256) norm_kernel(const Cx<R>* __restrict__ psi, int64_t count, double* partials, int* flag) {
+    __shared__ double scratch[32];
+    double s = 0.0;
+    bool bad = false;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        Cx<R> v = psi[i];
+        double p = double(v.x) * double(v.x) + double(v.y) * double(v.y);
+        if (!isfinite(p)) bad = true;
+        s += p;
+    }
+    if (bad) atomicExch(flag, 1);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) scratch[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) t += scratch[w];
+        partials[blockIdx.x] = t;
+    }
+}
+template <typename R>
+cudaError_t launch_norm(const Cx<R>* psi, int64_t count, double* partials, int* nblocks, int* flag, cudaStream_t s) {
+    int grid = int((count + 255) / 256);
+    if (grid > 152 * 8) grid = 152 * 8;
+    *nblocks = grid;
+    norm_kernel<R><<<grid, 256, 0, s>>>(psi, count, partials, flag);
+    return cudaGetLastError();
+}
+template cudaError_t launch_norm<float>(const Cx<float>*, int64_t, double*, int*, int*, cudaStream_t);
+template cudaError_t launch_norm<double>(const Cx<double>*, int64_t, double*, int*, int*, cudaStream_t);
+
+}  // namespace wfs

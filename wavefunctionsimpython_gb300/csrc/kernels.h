@@ -1,0 +1,113 @@
+// kernels.h — launch interface between the host engine (engine.cu) and the
+// device kernels. Plain structs; every launcher returns a cudaError_t.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace wfs {
+
+constexpr int kMaxBox = 8;      // volume-probability boxes per fused observation
+constexpr int kLocQ = 7;        // location box sums: S, Sx, Sy, Sz, Sxx, Syy, Szz
+
+enum PassOp { OP_PLAIN = 0, OP_KIN = 1, OP_VPH = 2, OP_OBS = 3 };
+
+struct ObsBox {
+    int b[3];
+    int c[3];
+};
+
+struct ObsArgs {
+    int nbox;
+    int has_loc;
+    ObsBox box[kMaxBox];
+    ObsBox loc;
+    int n[3];
+    double dx[3];
+    double* partials;   // [grid][nq] per-CTA sums (scratch)
+    int nq;             // nbox + (has_loc ? kLocQ : 0)
+};
+
+// One FFT pass over pencils of length L along one axis.
+// Strided kernels: element (outer o, row r, column c) lives at
+//   data + o*outer_stride + r*row_stride + c,   c < ncols (contiguous columns).
+// Contiguous kernels: row q (q < nrows) is data + q*L .. + L - 1.
+template <typename R>
+struct PassArgs {
+    Cx<R>* data;
+    const Cx<R>* tw;        // tw[m] = exp(-2 pi i m / L), m < L
+    int64_t outer_stride;
+    int64_t row_stride;
+    int32_t ncols;          // strided: columns per outer slab
+    int32_t tiles;          // strided: column tiles per outer slab
+    int64_t nrows;          // contiguous: number of rows
+    int32_t dir;            // OP_PLAIN: -1 forward, +1 inverse
+    R scale;                // applied to the pass output
+    // OP_KIN (strided): out = F^-1( k_row[k] * k_c1[c / c2n] * k_c2[c % c2n] * F(x) ) * scale
+    const Cx<R>* k_row;
+    const Cx<R>* k_c1;
+    const Cx<R>* k_c2;
+    int32_t c2n;
+    // OP_VPH (contiguous): out = F( e[q*L + z] * F^-1(x) ) * scale
+    const Cx<R>* ephase;
+    // OP_OBS (contiguous, read-only): observe scale * F^-1(x); rows are (x, y) = (q / ny, q % ny)
+    ObsArgs obs;
+};
+
+template <typename R>
+cudaError_t launch_fft_strided(int L, int op, const PassArgs<R>& a, int64_t outer_count, cudaStream_t s);
+template <typename R>
+cudaError_t launch_fft_contig(int L, int op, const PassArgs<R>& a, cudaStream_t s, int* grid_out);
+bool fft_length_supported(int L, bool dbl);
+int fft_contig_rows_per_cta(int L, bool dbl);
+int fft_strided_cols_per_cta(int L, bool dbl);
+
+// ---- field kernels (field_kernels.cu) ----
+struct WallDev {
+    float U, cx, cy, cz, nx, ny, nz, rx, ry, rz;
+    float plateau, slope, slope_exp, slit_spacing, slit_width;
+    int slit_count;
+};
+struct AbsorbDev {
+    float bottom[3], top[3], offset, pp[3], pn[3], ep[3], en[3];
+};
+
+cudaError_t launch_wall(float2* V, const int n[3], const float dx[3], const WallDev& w, cudaStream_t s);
+cudaError_t launch_absorbing(float2* V, const int n[3], const float dx[3], const AbsorbDev& a, cudaStream_t s);
+cudaError_t launch_add_raw(float2* V, const void* src, int raw_type, int64_t count, cudaStream_t s);
+template <typename R>
+cudaError_t launch_gaussian(Cx<R>* psi, const int n[3], const R* gx, const R* gy, const R* gz,
+                            const R* rx, const R* ry, const R* rz, R kx, R ky, R kz, cudaStream_t s);
+template <typename R>
+cudaError_t launch_vphase(Cx<R>* e, const float2* V, double dt, int64_t count, cudaStream_t s);
+template <typename R>
+cudaError_t launch_kin_product(Cx<R>* out, const Cx<R>* kx, const Cx<R>* ky, const Cx<R>* kz,
+                               const int n[3], cudaStream_t s);
+template <typename R>
+cudaError_t launch_mul_inplace(Cx<R>* inout, const Cx<R>* f, int64_t count, cudaStream_t s);
+template <typename R>
+cudaError_t launch_observe_real(const Cx<R>* psi, const ObsArgs& o, cudaStream_t s, int* grid_out);
+cudaError_t launch_reduce_partials(const double* partials, int nblocks, int nq, double* out, cudaStream_t s);
+template <typename R>
+cudaError_t launch_norm(const Cx<R>* psi, int64_t count, double* partials, int* nblocks, int* flag, cudaStream_t s);
+
+// ---- power series (taylor.cu) ----
+template <typename R>
+struct TaylorArgs {
+    const Cx<R>* s_prev;
+    Cx<R>* s_next;        // may be null on the last term
+    const float2* V;
+    const Cx<R>* acc_in;  // psi (term 1) or the accumulator
+    Cx<R>* acc_out;       // accumulator
+    int n[3];
+    R dxq;                // 2nd order: every axis divided by dx_x twice
+    R c4[3];              // 4th order: 1 / (12 dx_a^2)
+    R inv2m;              // 1 / 2 / m
+    R a;                  // dt / n
+};
+template <typename R>
+cudaError_t launch_taylor_term(int stencil_order, const TaylorArgs<R>& t, cudaStream_t s);
+
+}  // namespace wfs
