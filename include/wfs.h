@@ -154,11 +154,18 @@ enum wfs_pass_kind {
     WFS_PASS_OBSERVE = 4,   /* fused or standalone observation reduction */
     WFS_PASS_TAYLOR = 5,    /* one power-series term */
     WFS_PASS_OTHER = 6,     /* reductions, phase tables */
+    WFS_PASS_PLANE = 7,     /* yz planes: Fy^-1, Fz^-1, potential phase, Fz, Fy */
     WFS_NPASS = 8
 };
-/* on: 0 off, 1 on; a value > 1 also pre-creates that many event pairs. */
-int wfs_profile_enable(wfs_handle* h, int32_t on);
+/* stride: 0 off; k >= 1 brackets the launches of every k-th step (and the
+ * launches outside steps made while that step count is current). */
+int wfs_profile_enable(wfs_handle* h, int32_t stride);
 int wfs_profile_read(wfs_handle* h, double* ms_out, int64_t* count_out, int32_t reset);
+/* Split-step schedule (no counterpart in the reference). AUTO uses the fused
+ * yz-plane pass (2 HBM round trips per step) where the plane shape allows it,
+ * else one pass per axis (4 round trips); AXIS forces the per-axis passes. */
+enum wfs_schedule { WFS_SCHEDULE_AUTO = 0, WFS_SCHEDULE_AXIS = 1, WFS_SCHEDULE_PLANE = 2 };
+int wfs_set_schedule(wfs_handle* h, int32_t schedule);
 /* Number of kernels the engine has launched since creation. */
 int wfs_launch_count(wfs_handle* h, int64_t* out);
 

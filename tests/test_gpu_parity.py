@@ -99,12 +99,15 @@ def scenario(n, L, dbl, absorber=True):
     return dx, V, psi0
 
 
+@pytest.mark.parametrize("schedule", ["auto", "axis"])
 @pytest.mark.parametrize("dbl", [False, True])
-@pytest.mark.parametrize("n", [(32, 32, 32), (64, 64, 64), (16, 48, 32), (48, 48, 48), (96, 32, 64), (8, 128, 16)])
-def test_split_step(Engine, n, dbl):
+@pytest.mark.parametrize("n", [(32, 32, 32), (64, 64, 64), (16, 48, 32), (48, 48, 48), (96, 32, 64), (8, 128, 16),
+                               (16, 96, 96), (8, 128, 128), (4, 256, 256)])
+def test_split_step(Engine, n, dbl, schedule):
     L = tuple(0.4 * x for x in n)
     dx, V, psi0 = scenario(n, L, dbl)
     e = Engine(n, L, double_precision=dbl)
+    e.set_schedule(schedule)
     e.set_potential(V)
     e.set_psi(psi0)
     e.step_split(7, 0.01, 1.0)
@@ -189,7 +192,8 @@ def test_norm_and_nonfinite(Engine):
     n, L = (16, 16, 16), (12.0, 12.0, 12.0)
     e = Engine(n, L, double_precision=True)
     e.init_gaussian((1.5,) * 3, (0, 0, 0), (0, 0, 0))
-    assert abs(e.norm() - 1.0) < 1e-6
+    ref = orc.gaussian_wave_packet(n, orc.delta_x(L, n), (1.5,) * 3, (0, 0, 0), (0, 0, 0), True)
+    assert abs(e.norm() - np.sum(np.abs(ref) ** 2) * np.prod(orc.delta_x(L, n))) < 1e-12
     bad = e.get_psi()
     bad[3, 4, 5] = np.nan
     e.set_psi(bad)

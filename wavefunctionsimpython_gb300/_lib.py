@@ -33,9 +33,11 @@ EXPORTED = [
     "wfs_set_potential", "wfs_get_potential", "wfs_init_gaussian", "wfs_set_psi", "wfs_get_psi",
     "wfs_psi_device_ptr", "wfs_step_split", "wfs_step_taylor", "wfs_kinetic_operator", "wfs_potential_operator",
     "wfs_observe", "wfs_run_split", "wfs_norm", "wfs_profile_enable", "wfs_profile_read", "wfs_launch_count",
+    "wfs_set_schedule",
 ]
+SCHEDULES = {"auto": 0, "axis": 1, "plane": 2}
 NPASS = 8
-PASS_NAMES = ["x_kin", "y", "z_vph", "z", "observe", "taylor", "other", "unused"]
+PASS_NAMES = ["x_kin", "y", "z_vph", "z", "observe", "taylor", "other", "plane"]
 
 
 class WfsError(RuntimeError):
@@ -107,6 +109,7 @@ def load(path: str | os.PathLike | None = None):
         "wfs_profile_enable": ([vp, i32], C.c_int),
         "wfs_profile_read": ([vp, dp, C.POINTER(C.c_int64), i32], C.c_int),
         "wfs_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
+        "wfs_set_schedule": ([vp, i32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -225,8 +228,12 @@ class Engine:
             raise ValueError(f"psi shape {arr.shape} != grid {self.n}")
         self._ck(self.lib.wfs_set_psi(self.h, arr.ctypes.data, 0))
 
-    def get_psi(self) -> np.ndarray:
-        out = np.empty(self.n, dtype=self.dtype)
+    def get_psi(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Real-space psi copied to host memory (``out`` may be a pinned, C-contiguous buffer)."""
+        if out is None:
+            out = np.empty(self.n, dtype=self.dtype)
+        elif out.shape != self.n or out.dtype != np.dtype(self.dtype) or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous array of the grid's shape and dtype")
         self._ck(self.lib.wfs_get_psi(self.h, out.ctypes.data, 0))
         return out
 
@@ -290,9 +297,9 @@ class Engine:
                                         ls.ctypes.data_as(C.POINTER(C.c_double))))
         return ps[:nrec, :nb], ls[:nrec]
 
-    def profile_enable(self, on=True, capacity=0):
-        v = (max(int(capacity), 1) if capacity else 1) if on else 0
-        self._ck(self.lib.wfs_profile_enable(self.h, v))
+    def profile_enable(self, on=True, stride=1):
+        """Bracket the launches of every ``stride``-th step with CUDA events (0/False: off)."""
+        self._ck(self.lib.wfs_profile_enable(self.h, int(stride) if on else 0))
 
     def profile_read(self, reset=True):
         """Returns {pass name: (total ms, launches)} accumulated since the last reset."""
@@ -300,6 +307,10 @@ class Engine:
         cnt = (C.c_int64 * NPASS)()
         self._ck(self.lib.wfs_profile_read(self.h, ms, cnt, 1 if reset else 0))
         return {PASS_NAMES[k]: (ms[k], cnt[k]) for k in range(NPASS) if cnt[k]}
+
+    def set_schedule(self, name: str):
+        """'auto' (fused yz-plane pass where possible), 'axis' (one pass per axis) or 'plane'."""
+        self._ck(self.lib.wfs_set_schedule(self.h, SCHEDULES[name]))
 
     def launch_count(self) -> int:
         v = C.c_int64()

@@ -22,6 +22,7 @@
 
 #include "../../include/wfs.h"
 #include "kernels.h"
+#include "plane_kernels.cuh"
 
 using namespace wfs;
 
@@ -68,11 +69,14 @@ struct wfs_handle {
     std::string err;
     // per-pass CUDA-event profile (wfs_profile_enable / wfs_profile_read)
     bool prof_on;
+    int prof_stride;      // bracket the launches of every prof_stride-th step
+    int64_t steps_done;   // steps (split or power series) since creation
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_live;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_pool;
     double prof_ms[WFS_NPASS];
     int64_t prof_count[WFS_NPASS];
     int64_t launches;
+    int schedule;         // WFS_SCHEDULE_*
 };
 
 namespace {
@@ -99,7 +103,7 @@ struct PassScope {
     cudaEvent_t e1 = nullptr, e2 = nullptr;
     PassScope(wfs_handle* hh, int k) : h(hh), kind(k) {
         h->launches += 1;
-        if (!h->prof_on) return;
+        if (!h->prof_on || (h->steps_done % h->prof_stride) != 0) return;
         if (h->prof_pool.empty()) {
             cudaEvent_t a, b;
             if (cudaEventCreate(&a) != cudaSuccess) return;
@@ -146,6 +150,8 @@ int upload_roots(wfs_handle* h, int axis) {
 template <typename R>
 int ensure_kin(wfs_handle* h, KinTables& kt, double dt, double mass, double frac) {
     if (kt.dt == dt && kt.mass == mass && kt.frac == frac && kt.k[0]) return WFS_OK;
+    // kernels already queued on the engine's stream may still read the old table
+    if (kt.k[0]) CK(cudaStreamSynchronize(h->stream));
     for (int a = 0; a < 3; ++a) {
         const int L = h->n[a];
         std::vector<Cx<R>> v(L);
@@ -238,6 +244,27 @@ int pass_z_vph(wfs_handle* h) {
     return WFS_OK;
 }
 
+// Y[Fy^-1] Z[Fz^-1 E Fz] Y[Fy] in one launch (one cluster per yz-plane).
+template <typename R>
+int pass_plane(wfs_handle* h) {
+    PlaneArgs<R> a;
+    a.data = reinterpret_cast<Cx<R>*>(h->psi);
+    a.tw_y = reinterpret_cast<const Cx<R>*>(h->tw[1]);
+    a.tw_z = reinterpret_cast<const Cx<R>*>(h->tw[2]);
+    a.ephase = reinterpret_cast<const Cx<R>*>(h->ephase);
+    a.plane_elems = int64_t(h->n[1]) * h->n[2];
+    a.scale_y = R(1.0 / std::sqrt(double(h->n[1])));
+    a.scale_z = R(1.0 / double(h->n[2]));
+    PassScope ps(h, WFS_PASS_PLANE);
+    CK(launch_plane<R>(h->n[1], h->n[2], a, h->n[0], h->stream));
+    return WFS_OK;
+}
+
+bool use_plane(const wfs_handle* h) {
+    if (h->schedule == WFS_SCHEDULE_AXIS) return false;
+    return plane_pass_supported(h->n[1], h->n[2]);
+}
+
 // ---- representation changes ----------------------------------------------
 template <typename R>
 int finish_pending(wfs_handle* h) {
@@ -303,11 +330,16 @@ int split_steps(wfs_handle* h, int nsteps, double dt, double mass) {
     if ((rc = ensure_kin<R>(h, h->kin_full, dt, mass, 0.5))) return rc;
     bool merged = (h->rep == REP_PENDING);
     if (!merged && (rc = to_H<R>(h))) return rc;
-    for (int s = 0; s < nsteps; ++s) {
+    const bool plane = use_plane(h);
+    for (int s = 0; s < nsteps; ++s, ++h->steps_done) {
         if ((rc = pass_x_kin<R>(h, merged ? h->kin_full : h->kin_half))) return rc;
-        if ((rc = pass_y<R>(h, +1))) return rc;
-        if ((rc = pass_z_vph<R>(h))) return rc;
-        if ((rc = pass_y<R>(h, -1))) return rc;
+        if (plane) {
+            if ((rc = pass_plane<R>(h))) return rc;
+        } else {
+            if ((rc = pass_y<R>(h, +1))) return rc;
+            if ((rc = pass_z_vph<R>(h))) return rc;
+            if ((rc = pass_y<R>(h, -1))) return rc;
+        }
         merged = true;
     }
     h->rep = REP_PENDING;
@@ -462,7 +494,7 @@ int taylor_steps(wfs_handle* h, int nsteps, double dt, double mass, int order, i
     t.dxq = R(float(h->dx[0]));
     t.inv2m = R(1) / R(2) / R(mass);
     t.V = h->V;
-    for (int s = 0; s < nsteps; ++s) {
+    for (int s = 0; s < nsteps; ++s, ++h->steps_done) {
         Cx<R>* psi = reinterpret_cast<Cx<R>*>(h->psi);
         Cx<R>* A = reinterpret_cast<Cx<R>*>(h->scratch[0]);
         Cx<R>* B = reinterpret_cast<Cx<R>*>(h->scratch[1]);
@@ -527,7 +559,10 @@ int wfs_create(const wfs_grid_desc* d, wfs_handle** out) {
     h->dflag = nullptr;
     h->rep = REP_REAL;
     h->prof_on = false;
+    h->prof_stride = 1;
+    h->steps_done = 0;
     h->launches = 0;
+    h->schedule = WFS_SCHEDULE_AUTO;
     for (int k = 0; k < WFS_NPASS; ++k) { h->prof_ms[k] = 0.0; h->prof_count[k] = 0; }
     h->dtype = d->dtype;
     h->device = d->device;
@@ -874,11 +909,13 @@ int wfs_run_split(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t
                      : do_run_split<float>(h, nsteps, dt, mass, interval, boxes, nbox, loc, prob_series, loc_series);
 }
 
-int wfs_profile_enable(wfs_handle* h, int32_t on) {
+int wfs_profile_enable(wfs_handle* h, int32_t stride) {
     if (!h) return dispatch_err(h);
-    h->prof_on = on != 0;
-    // on > 1 is a capacity hint: create that many event pairs now, outside any timed region
-    while (on > 1 && int64_t(h->prof_pool.size()) < on) {
+    if (stride < 0) return set_err(h, WFS_ERR_ARG, "stride must be >= 0");
+    h->prof_on = stride != 0;
+    h->prof_stride = stride > 0 ? stride : 1;
+    // event pairs are created here, outside any timed region
+    while (h->prof_on && h->prof_pool.size() < 4096) {
         cudaEvent_t a, b;
         CK(cudaEventCreate(&a));
         CK(cudaEventCreate(&b));
@@ -904,6 +941,15 @@ int wfs_profile_read(wfs_handle* h, double* ms_out, int64_t* count_out, int32_t 
         if (count_out) count_out[k] = h->prof_count[k];
         if (reset) { h->prof_ms[k] = 0.0; h->prof_count[k] = 0; }
     }
+    return WFS_OK;
+}
+
+int wfs_set_schedule(wfs_handle* h, int32_t schedule) {
+    if (!h) return dispatch_err(h);
+    if (schedule < WFS_SCHEDULE_AUTO || schedule > WFS_SCHEDULE_PLANE) return set_err(h, WFS_ERR_ARG, "unknown schedule");
+    if (schedule == WFS_SCHEDULE_PLANE && !plane_pass_supported(h->n[1], h->n[2]))
+        return set_err(h, WFS_ERR_UNSUPPORTED, "plane schedule needs ny == nz in {32,48,64,96,128,192,256,384,512}");
+    h->schedule = schedule;
     return WFS_OK;
 }
 

@@ -72,16 +72,54 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[NQ], int nq, do
     }
 }
 
-// Accumulate |psi|^2 of one element at (x, y, z) into the observation sums.
-// wxy[b] and the location-row factors are per-row constants set by the caller.
+// Observation sums. A thread first sums the few elements of one (x, y) row it
+// holds in the working precision (RowAcc: Simpson z-weight * |psi|^2 per box,
+// and the location moments in z), then folds the row into FP64 sums with the
+// row's x/y weights (obs_row_flush). FP64 work is thus per row and per thread,
+// not per element: GB300's FP64 rate is a small fraction of its FP32 rate.
 template <typename R>
-struct ObsAcc {
-    double acc[kMaxBox + kLocQ];
+struct RowAcc {
+    R box[kMaxBox];
+    R s0, sz, szz;
     __device__ __forceinline__ void zero() {
 #pragma unroll
-        for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = 0.0;
+        for (int b = 0; b < kMaxBox; ++b) box[b] = R(0);
+        s0 = sz = szz = R(0);
     }
 };
+
+template <typename R>
+__device__ __forceinline__ void obs_row_element(const ObsArgs& o, RowAcc<R>& ra, int z, Cx<R> v) {
+    const R p = v.x * v.x + v.y * v.y;
+#pragma unroll
+    for (int b = 0; b < kMaxBox; ++b)
+        if (b < o.nbox) ra.box[b] += simpson_w<R>(z, o.box[b].b[2], o.box[b].c[2]) * p;
+    if (o.has_loc) {
+        const R w = simpson_w<R>(z, o.loc.b[2], o.loc.c[2]) * p;
+        const R rz = R(o.dx[2]) * R(z - o.n[2] / 2);
+        ra.s0 += w;
+        ra.sz += w * rz;
+        ra.szz += w * rz * rz;
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void obs_row_flush(const ObsArgs& o, double (&acc)[kMaxBox + kLocQ], const RowAcc<R>& ra,
+                                              const R (&wxy)[kMaxBox], R lxy, R rx, R ry) {
+#pragma unroll
+    for (int b = 0; b < kMaxBox; ++b)
+        if (b < o.nbox) acc[b] += double(wxy[b]) * double(ra.box[b]);
+    if (o.has_loc && lxy != R(0)) {
+        const double l = double(lxy), s0 = double(ra.s0), x = double(rx), y = double(ry);
+        acc[kMaxBox + 0] += l * s0;
+        acc[kMaxBox + 1] += l * x * s0;
+        acc[kMaxBox + 2] += l * y * s0;
+        acc[kMaxBox + 3] += l * double(ra.sz);
+        acc[kMaxBox + 4] += l * x * x * s0;
+        acc[kMaxBox + 5] += l * y * y * s0;
+        acc[kMaxBox + 6] += l * double(ra.szz);
+    }
+}
 
 template <typename R>
 __device__ __forceinline__ void obs_row_factors(const ObsArgs& o, int x, int y, R (&wxy)[kMaxBox], R& lxy,
@@ -99,30 +137,6 @@ __device__ __forceinline__ void obs_row_factors(const ObsArgs& o, int x, int y, 
     }
     rx = R(o.dx[0]) * R(x - o.n[0] / 2);
     ry = R(o.dx[1]) * R(y - o.n[1] / 2);
-}
-
-template <typename R>
-__device__ __forceinline__ void obs_element(const ObsArgs& o, double (&acc)[kMaxBox + kLocQ], const R (&wxy)[kMaxBox],
-                                            R lxy, R rx, R ry, int z, Cx<R> v) {
-    R p = v.x * v.x + v.y * v.y;
-#pragma unroll
-    for (int b = 0; b < kMaxBox; ++b) {
-        if (b < o.nbox) acc[b] += double(wxy[b] * simpson_w<R>(z, o.box[b].b[2], o.box[b].c[2]) * p);
-    }
-    if (o.has_loc) {
-        R w = lxy * simpson_w<R>(z, o.loc.b[2], o.loc.c[2]) * p;
-        if (w != R(0)) {
-            R rz = R(o.dx[2]) * R(z - o.n[2] / 2);
-            double wd = double(w);
-            acc[kMaxBox + 0] += wd;
-            acc[kMaxBox + 1] += wd * double(rx);
-            acc[kMaxBox + 2] += wd * double(ry);
-            acc[kMaxBox + 3] += wd * double(rz);
-            acc[kMaxBox + 4] += wd * double(rx) * double(rx);
-            acc[kMaxBox + 5] += wd * double(ry) * double(ry);
-            acc[kMaxBox + 6] += wd * double(rz) * double(rz);
-        }
-    }
 }
 
 // Compacts the fixed accumulator layout to [nbox probs][loc sums] and stores per-CTA partials.
@@ -246,8 +260,11 @@ __global__ void __launch_bounds__(cmax(P, Q) * W) fft_contig_kernel(const PassAr
             const int x = int(row / o.n[1]), y = int(row % o.n[1]);
             R wxy[kMaxBox], lxy, rx, ry;
             obs_row_factors<R>(o, x, y, wxy, lxy, rx, ry);
+            RowAcc<R> ra;
+            ra.zero();
 #pragma unroll
-            for (int k = 0; k < P; ++k) obs_element<R>(o, acc, wxy, lxy, rx, ry, t + Q * k, scale(a2[k], a.scale));
+            for (int k = 0; k < P; ++k) obs_row_element<R>(o, ra, t + Q * k, scale(a2[k], a.scale));
+            obs_row_flush<R>(o, acc, ra, wxy, lxy, rx, ry);
         }
         __syncthreads();
         obs_store(a.obs, acc, reinterpret_cast<double*>(smem_raw));

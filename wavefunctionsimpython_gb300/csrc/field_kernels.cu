@@ -373,7 +373,10 @@ __global__ void __launch_bounds__(256) observe_real_kernel(const Cx<R>* __restri
         R wxy[kMaxBox], lxy, rx, ry;
         obs_row_factors<R>(o, x, y, wxy, lxy, rx, ry);
         const Cx<R>* rp = psi + row * o.n[2];
-        for (int z = lane; z < o.n[2]; z += 32) obs_element<R>(o, acc, wxy, lxy, rx, ry, z, rp[z]);
+        RowAcc<R> ra;
+        ra.zero();
+        for (int z = lane; z < o.n[2]; z += 32) obs_row_element<R>(o, ra, z, rp[z]);
+        obs_row_flush<R>(o, acc, ra, wxy, lxy, rx, ry);
     }
     obs_store(o, acc, scratch);
 }

@@ -1,0 +1,134 @@
+// host_helpers.h — host-side pieces shared by the single-grid engine and the batch engine.
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/wfs.h"
+#include "kernels.h"
+
+namespace wfs {
+
+// Per-axis envelope g_d(i) and coordinate r_d(i) of the Gaussian packet
+// (common.cu:569-586, gaussian_wave_packet.cu:36-40), computed in the
+// working precision with the reference's operation order; the device kernel
+// multiplies them per voxel.
+template <typename R>
+inline void gaussian_axes(const int n[3], const double dx[3], const double sigma[3], const double r0[3],
+                          std::vector<R>& g, std::vector<R>& r) {
+    const int total = n[0] + n[1] + n[2];
+    g.assign(total, R(0));
+    r.assign(total, R(0));
+    const int off[3] = {0, n[0], n[0] + n[1]};
+    for (int a = 0; a < 3; ++a) {
+        for (int i = 0; i < n[a]; ++i) {
+            const int iv = i - n[a] / 2;
+            if (sizeof(R) == 8) {
+                const double rr = dx[a] * double(iv);
+                const double aa = 2.0 * sigma[a];
+                const double norm = std::pow(2.0 / M_PI / aa / aa, 0.25);
+                const double d = rr - r0[a];
+                g[off[a] + i] = R(norm * std::exp(-d * d / aa / aa));
+                r[off[a] + i] = R(rr);
+            } else {
+                volatile float rr = float(dx[a]) * float(iv);
+                const float aa = 2.0f * float(sigma[a]);
+                volatile float q = 2.0f / float(M_PI);
+                q = q / aa;
+                q = q / aa;
+                const float norm = std::pow(float(q), 0.25f);
+                volatile float d = float(rr) - float(r0[a]);
+                volatile float ex = -float(d) * float(d);
+                ex = ex / aa;
+                ex = ex / aa;
+                volatile float gg = norm * std::exp(float(ex));
+                g[off[a] + i] = R(float(gg));
+                r[off[a] + i] = R(float(rr));
+            }
+        }
+    }
+}
+
+// Float32 frame of a wall (potential_wall.cu:39-45, common.cu:348-369) with
+// every product and sum rounded separately, as the reference's device code does.
+inline bool wall_frame(const wfs_wall* w, WallDev& wd) {
+    const double nn = std::sqrt(w->normal[0] * w->normal[0] + w->normal[1] * w->normal[1] + w->normal[2] * w->normal[2]);
+    if (!(nn > 0)) return false;
+    auto mul = [](float a, float b) { volatile float r = a * b; return float(r); };
+    auto add = [](float a, float b) { volatile float r = a + b; return float(r); };
+    auto sub = [](float a, float b) { volatile float r = a - b; return float(r); };
+    const float n[3] = {float(w->normal[0] / nn), float(w->normal[1] / nn), float(w->normal[2] / nn)};
+    float up[3] = {0.f, 1.f, 0.f};
+    const float nd = add(add(mul(n[0], up[0]), mul(n[1], up[1])), mul(n[2], up[2]));
+    if (std::fabs(nd) > 0.99f) { up[0] = 0.f; up[2] = 1.f; }
+    const float c[3] = {sub(mul(n[1], up[2]), mul(n[2], up[1])), sub(mul(n[2], up[0]), mul(n[0], up[2])),
+                        sub(mul(n[0], up[1]), mul(n[1], up[0]))};
+    const float cc = add(add(mul(c[0], c[0]), mul(c[1], c[1])), mul(c[2], c[2]));
+    const float ln = float(std::sqrt(double(cc)));
+    if (!(ln > 0)) return false;
+    float right[3];
+    for (int i = 0; i < 3; ++i) { volatile float r = c[i] / ln; right[i] = r; }
+    volatile float half = float(w->slit_rotation) / 2.0f;
+    const float q0 = float(std::cos(double(half)));
+    const float s = float(std::sin(double(half)));
+    const float q1 = mul(s, n[0]), q2 = mul(s, n[1]), q3 = mul(s, n[2]);
+    float Q[3][3];
+    Q[0][0] = sub(sub(add(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
+    Q[0][1] = mul(2.f, sub(mul(q1, q2), mul(q0, q3)));
+    Q[0][2] = mul(2.f, add(mul(q1, q3), mul(q0, q2)));
+    Q[1][0] = mul(2.f, add(mul(q2, q1), mul(q0, q3)));
+    Q[1][1] = sub(add(sub(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
+    Q[1][2] = mul(2.f, sub(mul(q2, q3), mul(q0, q1)));
+    Q[2][0] = mul(2.f, sub(mul(q3, q1), mul(q0, q2)));
+    Q[2][1] = mul(2.f, add(mul(q3, q2), mul(q0, q1)));
+    Q[2][2] = add(sub(sub(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
+    float rr[3];
+    for (int i = 0; i < 3; ++i) rr[i] = add(add(mul(Q[i][0], right[0]), mul(Q[i][1], right[1])), mul(Q[i][2], right[2]));
+    wd.U = float(w->potential_hartree);
+    wd.cx = float(w->center[0]); wd.cy = float(w->center[1]); wd.cz = float(w->center[2]);
+    wd.nx = n[0]; wd.ny = n[1]; wd.nz = n[2];
+    wd.rx = rr[0]; wd.ry = rr[1]; wd.rz = rr[2];
+    wd.plateau = float(w->plateau_thickness);
+    wd.slope = float(w->slope_thickness);
+    wd.slope_exp = float(w->slope_exponent);
+    wd.slit_count = w->slit_count < 0 ? 0 : (w->slit_count > 4 ? 4 : w->slit_count);
+    wd.slit_spacing = float(w->slit_spacing);
+    wd.slit_width = float(w->slit_width);
+    return true;
+}
+
+inline AbsorbDev absorbing_dev(const wfs_absorbing* a) {
+    AbsorbDev ad;
+    for (int i = 0; i < 3; ++i) {
+        ad.bottom[i] = float(a->bottom[i]);
+        ad.top[i] = float(a->top[i]);
+        ad.pp[i] = float(a->potential_pos[i]);
+        ad.pn[i] = float(a->potential_neg[i]);
+        ad.ep[i] = float(a->exponent_pos[i]);
+        ad.en[i] = float(a->exponent_neg[i]);
+    }
+    ad.offset = float(a->offset);
+    return ad;
+}
+
+// exp(-i k^2 dt frac / m) for k = 2 pi fftfreq(L, dx), in precision R.
+template <typename R>
+inline void kinetic_axis(int L, double dx, double dt, double mass, double frac, Cx<R>* out) {
+    for (int i = 0; i < L; ++i) {
+        const int fi = (i < (L + 1) / 2) ? i : i - L;
+        const double k = 2.0 * M_PI * double(fi) / (double(L) * dx);
+        const double ang = -k * k * dt * frac / mass;
+        out[i] = mk<R>(R(std::cos(ang)), R(std::sin(ang)));
+    }
+}
+
+template <typename R>
+inline void roots_table(int L, Cx<R>* out) {
+    for (int m = 0; m < L; ++m) {
+        const double a = -2.0 * M_PI * double(m) / double(L);
+        out[m] = mk<R>(R(std::cos(a)), R(std::sin(a)));
+    }
+}
+
+}  // namespace wfs

@@ -64,6 +64,13 @@ bool fft_length_supported(int L, bool dbl);
 int fft_contig_rows_per_cta(int L, bool dbl);
 int fft_strided_cols_per_cta(int L, bool dbl);
 
+// ---- fused yz-plane pass (plane_f32.cu / plane_f64.cu) ----
+template <typename R>
+struct PlaneArgs;
+template <typename R>
+cudaError_t launch_plane(int ny, int nz, const PlaneArgs<R>& a, int64_t nplanes, cudaStream_t s);
+bool plane_pass_supported(int ny, int nz);
+
 // ---- field kernels (field_kernels.cu) ----
 struct WallDev {
     float U, cx, cy, cz, nx, ny, nz, rx, ry, rz;
