@@ -169,6 +169,46 @@ int wfs_set_schedule(wfs_handle* h, int32_t schedule);
 /* Number of kernels the engine has launched since creation. */
 int wfs_launch_count(wfs_handle* h, int64_t* out);
 
+/* ------------------------------------------------------------------------
+ * Batched sweep: many independent packets on uneven cubic grids advanced
+ * together (no counterpart in the reference, which runs one simulation per
+ * process, sources/core_sim.py:26-65; each instance follows the same split
+ * step as wfs_step_split). complex64 only; sizes 32, 48, 64, 96, 128. One
+ * kernel launch per step advances every instance; runs can be captured in a
+ * CUDA graph. Instance builders mirror the single-grid ones.
+ * ---------------------------------------------------------------------- */
+typedef struct wfs_batch wfs_batch;
+typedef struct {
+    int32_t ninst;
+    const int32_t* n;        /* ninst cube edge lengths */
+    const double* extent;    /* ninst cube edge lengths in Bohr radii */
+    int32_t device;
+    void* stream;            /* cudaStream_t or NULL */
+} wfs_batch_desc;
+
+int wfs_batch_create(const wfs_batch_desc* desc, wfs_batch** out);
+int wfs_batch_destroy(wfs_batch* b);
+const char* wfs_batch_last_error(const wfs_batch* b);
+int wfs_batch_synchronize(wfs_batch* b);
+int wfs_batch_init_gaussian(wfs_batch* b, int32_t i, const double sigma[3], const double r0[3], const double k0[3]);
+int wfs_batch_add_wall(wfs_batch* b, int32_t i, const wfs_wall* w);
+int wfs_batch_add_absorbing(wfs_batch* b, int32_t i, const wfs_absorbing* a);
+int wfs_batch_set_potential(wfs_batch* b, int32_t i, const void* v_c64, int32_t on_device);
+int wfs_batch_set_psi(wfs_batch* b, int32_t i, const void* psi_c64, int32_t on_device);
+int wfs_batch_get_psi(wfs_batch* b, int32_t i, void* psi_c64, int32_t to_device);
+/* nsteps Strang steps of every instance; use_graph != 0 replays a captured CUDA graph. */
+int wfs_batch_run(wfs_batch* b, int32_t nsteps, double dt, double mass, int32_t use_graph);
+/* One Simpson volume probability per instance: boxes[i] -> prob_out[i]. */
+int wfs_batch_observe(wfs_batch* b, const wfs_box* boxes, double* prob_out);
+/* Cluster size (1, 2, 4, 8, 16) and radix orientation (0: P >= Q, 1: swapped) of the step kernel. */
+int wfs_batch_set_config(wfs_batch* b, int32_t cluster, int32_t swap);
+/* Times every configuration over `steps` steps and keeps the fastest (psi is restored);
+ * ms_out (optional, 10 entries) receives ms per step for cluster {1,2,4,8,16} x swap {0,1},
+ * -1 where a configuration cannot be scheduled. */
+int wfs_batch_autotune(wfs_batch* b, double dt, double mass, int32_t steps, int32_t* cluster_out, int32_t* swap_out,
+                       double* ms_out);
+int wfs_batch_launch_count(wfs_batch* b, int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

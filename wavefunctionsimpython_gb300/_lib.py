@@ -34,6 +34,10 @@ EXPORTED = [
     "wfs_psi_device_ptr", "wfs_step_split", "wfs_step_taylor", "wfs_kinetic_operator", "wfs_potential_operator",
     "wfs_observe", "wfs_run_split", "wfs_norm", "wfs_profile_enable", "wfs_profile_read", "wfs_launch_count",
     "wfs_set_schedule",
+    "wfs_batch_create", "wfs_batch_destroy", "wfs_batch_last_error", "wfs_batch_synchronize",
+    "wfs_batch_init_gaussian", "wfs_batch_add_wall", "wfs_batch_add_absorbing", "wfs_batch_set_potential",
+    "wfs_batch_set_psi", "wfs_batch_get_psi", "wfs_batch_run", "wfs_batch_observe", "wfs_batch_set_config",
+    "wfs_batch_autotune", "wfs_batch_launch_count",
 ]
 SCHEDULES = {"auto": 0, "axis": 1, "plane": 2}
 NPASS = 8
@@ -66,6 +70,11 @@ class AbsorbingDesc(C.Structure):
 
 class Box(C.Structure):
     _fields_ = [("bottom", C.c_int32 * 3), ("count", C.c_int32 * 3)]
+
+
+class BatchDesc(C.Structure):
+    _fields_ = [("ninst", C.c_int32), ("n", C.POINTER(C.c_int32)), ("extent", C.POINTER(C.c_double)),
+                ("device", C.c_int32), ("stream", C.c_void_p)]
 
 
 _lib = None
@@ -110,6 +119,21 @@ def load(path: str | os.PathLike | None = None):
         "wfs_profile_read": ([vp, dp, C.POINTER(C.c_int64), i32], C.c_int),
         "wfs_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "wfs_set_schedule": ([vp, i32], C.c_int),
+        "wfs_batch_create": ([C.POINTER(BatchDesc), C.POINTER(vp)], C.c_int),
+        "wfs_batch_destroy": ([vp], C.c_int),
+        "wfs_batch_last_error": ([vp], C.c_char_p),
+        "wfs_batch_synchronize": ([vp], C.c_int),
+        "wfs_batch_init_gaussian": ([vp, i32, dp, dp, dp], C.c_int),
+        "wfs_batch_add_wall": ([vp, i32, C.POINTER(WallDesc)], C.c_int),
+        "wfs_batch_add_absorbing": ([vp, i32, C.POINTER(AbsorbingDesc)], C.c_int),
+        "wfs_batch_set_potential": ([vp, i32, vp, i32], C.c_int),
+        "wfs_batch_set_psi": ([vp, i32, vp, i32], C.c_int),
+        "wfs_batch_get_psi": ([vp, i32, vp, i32], C.c_int),
+        "wfs_batch_run": ([vp, i32, dbl, dbl, i32], C.c_int),
+        "wfs_batch_observe": ([vp, C.POINTER(Box), dp], C.c_int),
+        "wfs_batch_set_config": ([vp, i32, i32], C.c_int),
+        "wfs_batch_autotune": ([vp, dbl, dbl, i32, C.POINTER(i32), C.POINTER(i32), dp], C.c_int),
+        "wfs_batch_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -320,4 +344,105 @@ class Engine:
     def norm(self) -> float:
         v = C.c_double()
         self._ck(self.lib.wfs_norm(self.h, C.byref(v)))
+        return v.value
+
+
+class Batch:
+    """Many independent wave packets on uneven cubic grids, advanced together (complex64)."""
+
+    def __init__(self, sizes, extents, device=0, stream=None):
+        self.lib = load()
+        self.sizes = [int(s) for s in sizes]
+        self.extents = [float(e) for e in extents]
+        self.ninst = len(self.sizes)
+        n = (C.c_int32 * self.ninst)(*self.sizes)
+        ext = (C.c_double * self.ninst)(*self.extents)
+        d = BatchDesc(self.ninst, n, ext, int(device), stream)
+        h = C.c_void_p()
+        rc = self.lib.wfs_batch_create(C.byref(d), C.byref(h))
+        if rc != WFS_OK:
+            raise WfsError(rc, self.lib.wfs_batch_last_error(None).decode())
+        self.h = h
+
+    def _ck(self, rc):
+        if rc != WFS_OK:
+            raise WfsError(rc, self.lib.wfs_batch_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wfs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_gaussian(self, i, sigma, r0, k0):
+        self._ck(self.lib.wfs_batch_init_gaussian(self.h, int(i), _d3(sigma), _d3(r0), _d3(k0)))
+
+    def add_wall(self, i, potential_hartree, center, normal, plateau, slope=0.0, slope_exponent=1.0,
+                 slit_count=0, slit_spacing=1.0, slit_width=0.5, slit_rotation=0.0):
+        w = WallDesc(float(potential_hartree), _d3(center), _d3(normal), float(plateau), float(slope),
+                     float(slope_exponent), int(slit_count), float(slit_spacing), float(slit_width), float(slit_rotation))
+        self._ck(self.lib.wfs_batch_add_wall(self.h, int(i), C.byref(w)))
+
+    def add_absorbing(self, i, bottom, top, offset, potential_pos, potential_neg, exponent_pos, exponent_neg):
+        a = AbsorbingDesc(_d3(bottom), _d3(top), float(offset), _d3(potential_pos), _d3(potential_neg),
+                          _d3(exponent_pos), _d3(exponent_neg))
+        self._ck(self.lib.wfs_batch_add_absorbing(self.h, int(i), C.byref(a)))
+
+    def set_potential(self, i, V):
+        arr = np.ascontiguousarray(V, dtype=np.complex64)
+        L = self.sizes[i]
+        if arr.shape != (L, L, L):
+            raise ValueError("potential shape mismatch")
+        self._ck(self.lib.wfs_batch_set_potential(self.h, int(i), arr.ctypes.data, 0))
+
+    def set_psi(self, i, psi):
+        arr = np.ascontiguousarray(psi, dtype=np.complex64)
+        L = self.sizes[i]
+        if arr.shape != (L, L, L):
+            raise ValueError("psi shape mismatch")
+        self._ck(self.lib.wfs_batch_set_psi(self.h, int(i), arr.ctypes.data, 0))
+
+    def get_psi(self, i):
+        L = self.sizes[i]
+        out = np.empty((L, L, L), dtype=np.complex64)
+        self._ck(self.lib.wfs_batch_get_psi(self.h, int(i), out.ctypes.data, 0))
+        return out
+
+    def run(self, nsteps, dt, mass=1.0, graph=True):
+        self._ck(self.lib.wfs_batch_run(self.h, int(nsteps), float(dt), float(mass), 1 if graph else 0))
+
+    def synchronize(self):
+        self._ck(self.lib.wfs_batch_synchronize(self.h))
+
+    def observe(self, boxes):
+        """boxes: list of (bottom_voxel, count), one per instance -> probabilities."""
+        if len(boxes) != self.ninst:
+            raise ValueError("one box per instance")
+        arr = (Box * self.ninst)()
+        for i, (b, c) in enumerate(boxes):
+            arr[i] = make_box(b, c)
+        out = (C.c_double * self.ninst)()
+        self._ck(self.lib.wfs_batch_observe(self.h, arr, out))
+        return np.array(out[:])
+
+    def set_config(self, cluster, swap=0):
+        self._ck(self.lib.wfs_batch_set_config(self.h, int(cluster), int(swap)))
+
+    def autotune(self, dt, mass=1.0, steps=5):
+        """Times cluster {1,2,4,8,16} x radix orientation {0,1}; keeps the fastest.
+        Returns (cluster, swap, table of ms per step)."""
+        cl, sw = C.c_int32(), C.c_int32()
+        ms = (C.c_double * 10)()
+        self._ck(self.lib.wfs_batch_autotune(self.h, float(dt), float(mass), int(steps), C.byref(cl), C.byref(sw), ms))
+        table = {(c, s): ms[s * 5 + k] for s in (0, 1) for k, c in enumerate((1, 2, 4, 8, 16))}
+        return cl.value, sw.value, table
+
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        self._ck(self.lib.wfs_batch_launch_count(self.h, C.byref(v)))
         return v.value
