@@ -209,6 +209,26 @@ int wfs_batch_autotune(wfs_batch* b, double dt, double mass, int32_t steps, int3
                        double* ms_out);
 int wfs_batch_launch_count(wfs_batch* b, int64_t* out);
 
+/* ------------------------------------------------------------------------
+ * Allocation-free observation. No counterpart in the reference: it exists for
+ * callers that may not allocate device memory (a host application whose own
+ * allocator owns the GPU, real-time loops that must not take allocator locks,
+ * plugins that only receive device pointers) and so cannot create a handle.
+ * Same results as wfs_observe for a real-space psi the caller owns on the
+ * current device: out_device[0..nbox) = volume probabilities, and when loc is
+ * not NULL out_device[nbox..nbox+3) = <r>, out_device[nbox+3..nbox+6) = <r^2>.
+ * Asynchronous on `stream` (NULL = legacy default stream); calls no
+ * allocating routine. Scratch is one fixed device array of
+ * WFS_NOALLOC_SCRATCH_DOUBLES doubles (1 MiB per GPU, held until exit):
+ * grids with ceil(nx*ny/8) * (nbox + (loc ? 7 : 0)) > WFS_NOALLOC_SCRATCH_DOUBLES - 16
+ * are rejected with WFS_ERR_UNSUPPORTED. The first call on a device looks up
+ * the array's address (make it before any stream capture). Calls share the
+ * array: calls that overlap on the GPU race. Message: wfs_global_error().
+ * ---------------------------------------------------------------------- */
+#define WFS_NOALLOC_SCRATCH_DOUBLES 131072
+int wfs_observe_noalloc(const void* psi_device, int32_t dtype, const int32_t n[3], const double extent[3],
+                        const wfs_box* boxes, int32_t nbox, const wfs_box* loc, double* out_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

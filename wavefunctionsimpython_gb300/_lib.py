@@ -37,7 +37,7 @@ EXPORTED = [
     "wfs_batch_create", "wfs_batch_destroy", "wfs_batch_last_error", "wfs_batch_synchronize",
     "wfs_batch_init_gaussian", "wfs_batch_add_wall", "wfs_batch_add_absorbing", "wfs_batch_set_potential",
     "wfs_batch_set_psi", "wfs_batch_get_psi", "wfs_batch_run", "wfs_batch_observe", "wfs_batch_set_config",
-    "wfs_batch_autotune", "wfs_batch_launch_count",
+    "wfs_batch_autotune", "wfs_batch_launch_count", "wfs_observe_noalloc",
 ]
 SCHEDULES = {"auto": 0, "axis": 1, "plane": 2}
 NPASS = 8
@@ -134,6 +134,7 @@ def load(path: str | os.PathLike | None = None):
         "wfs_batch_set_config": ([vp, i32, i32], C.c_int),
         "wfs_batch_autotune": ([vp, dbl, dbl, i32, C.POINTER(i32), C.POINTER(i32), dp], C.c_int),
         "wfs_batch_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
+        "wfs_observe_noalloc": ([vp, i32, C.POINTER(i32), dp, C.POINTER(Box), i32, C.POINTER(Box), dp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -39,6 +39,11 @@ struct KinTables {
 
 }  // namespace
 
+namespace wfs {
+// Lets entry points without a handle report through wfs_global_error().
+void record_global_error(const std::string& m) { g_error = m; }
+}  // namespace wfs
+
 struct wfs_handle {
     int n[3];
     double extent[3];
