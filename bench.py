@@ -48,7 +48,19 @@ SIGMA, R0, K0 = (3.0, 3.0, 3.0), (-20.0, 0.0, 0.0), (2.5, 0.0, 0.0)
 ABS_CELLS = 16
 ABS_POT = -50.0
 METRIC = "site-steps/s at 256^3 c64 (split-step, double slit)"
-PROFILE_STRIDE = 10  # per-launch CUDA events on every 10th step of the timed region
+PROFILE_STRIDE = 10  # per-launch CUDA events on every 10th step of long timed regions
+
+
+def profile_stride(steps):
+    """Event sampling stride: every 10th step of long runs, every step of short ones."""
+    return PROFILE_STRIDE if steps >= 20 * PROFILE_STRIDE else 1
+
+
+def engine_stream(torch):
+    """A dedicated (non-default) stream shared by the engine and the timing events."""
+    s = torch.cuda.Stream()
+    torch.cuda.set_stream(s)
+    return s
 
 
 def workload_config():
@@ -229,7 +241,7 @@ def run_own(args):
     world, rank, local, pg = dist_setup(args)
     dev = local if world > 1 else args.device
     torch.cuda.set_device(dev)
-    stream = torch.cuda.current_stream()
+    stream = engine_stream(torch)
     box = transmitted_box()
     e = build_engine(dev, stream.cuda_stream)
     e.set_schedule(args.schedule)
@@ -238,7 +250,7 @@ def run_own(args):
     e.run_split(max(args.warmup, 1), DT, 1.0, OBS_INTERVAL, [box], None)
     torch.cuda.synchronize()
     e.profile_read(reset=True)
-    e.profile_enable(True, stride=PROFILE_STRIDE)
+    e.profile_enable(True, stride=profile_stride(args.steps))
     launches0 = e.launch_count()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
@@ -327,14 +339,14 @@ def run_taylor(args):
     r = np.arange(n) * dx - L / 2
     V = (0.5 * 0.25 * (r[:, None, None] ** 2 + r[None, :, None] ** 2 + r[None, None, :] ** 2)).astype(np.complex64)
     torch.cuda.set_device(args.device)
-    stream = torch.cuda.current_stream()
+    stream = engine_stream(torch)
     e = Engine((n, n, n), (L,) * 3, device=args.device, stream=stream.cuda_stream)
     e.set_potential(V)
     e.init_gaussian((1.5,) * 3, (5.0, 0.0, 0.0), (0.0, 0.0, 0.0))
     e.step_taylor(args.warmup, 0.005, 1.0, order, 4)
     torch.cuda.synchronize()
     e.profile_read(reset=True)
-    e.profile_enable(True, stride=PROFILE_STRIDE)
+    e.profile_enable(True, stride=profile_stride(args.steps))
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(args.device) as clk:
         torch.cuda.synchronize()
@@ -375,7 +387,7 @@ def run_batch(args):
     rng = np.random.default_rng(2024)
     sizes = [n for n, cnt in BATCH_MIX for _ in range(cnt)]
     torch.cuda.set_device(args.device)
-    stream = torch.cuda.current_stream()
+    stream = engine_stream(torch)
     b = Batch(sizes, [40.0] * len(sizes), device=args.device, stream=stream.cuda_stream)
     for i, n in enumerate(sizes):
         U, w = rng.uniform(0.2, 2.0), rng.uniform(1.0, 4.0)

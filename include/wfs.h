@@ -138,6 +138,15 @@ int wfs_run_split(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t
                   const wfs_box* boxes, int32_t nbox, const wfs_box* loc,
                   double* prob_series, double* loc_series);
 
+/* Probability flux through a sampled plane: PlaneProbabilityCurrent.calculate
+ * (sources/measurement.py:258-289, probability_current_density.cu:11-218).
+ * count[2] are the (odd) Simpson sample counts, size[2] the plane's extent in
+ * Bohr radii. flux_out = integral of j.n over the plane; density_out (optional,
+ * count[0]*count[1] values in psi's real precision, to host or device memory)
+ * receives the sampled current density. */
+int wfs_plane_current(wfs_handle* h, const double center[3], const double normal[3], const double size[2],
+                      const int32_t count[2], double mass, double* flux_out, void* density_out, int32_t to_device);
+
 /* FP64 norm sum |psi|^2 dV over the whole grid; WFS_ERR_NONFINITE when psi holds NaN/Inf. */
 int wfs_norm(wfs_handle* h, double* norm_out);
 

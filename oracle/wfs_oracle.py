@@ -756,3 +756,89 @@ def config3_double_slit(n=256, extent=80.0):
                     absorbing=Absorbing(bottom=(-inner,) * 3, top=(inner,) * 3, offset=0.0,
                                         potential_pos=(-50.0,) * 3, potential_neg=(-50.0,) * 3,
                                         exponent_pos=(2.0,) * 3, exponent_neg=(2.0,) * 3))
+
+
+# ---------------------------------------------------------------------------
+# Plane probability current — sources/cuda_kernels/probability_current_density.cu:11-218,
+#                              sources/measurement.py:207-289
+# ---------------------------------------------------------------------------
+
+def plane_frame(normal):
+    """right/up of the sampling plane (probability_current_density.cu:41-49), float32:
+    prefUp = (0,1,0), or (0,0,1) when |n.y| > 0.99; right = normalize(n x prefUp);
+    up = normalize(right x n)."""
+    f = np.float32
+    n = np.asarray(normal, dtype=np.float64)
+    n = (n / math.sqrt(float(np.dot(n, n)))).astype(np.float32)
+    pu = np.array([0.0, 1.0, 0.0], dtype=np.float32)
+    d = f(f(f(n[0] * pu[0]) + f(n[1] * pu[1])) + f(n[2] * pu[2]))
+    if abs(float(d)) > 0.99:
+        pu = np.array([0.0, 0.0, 1.0], dtype=np.float32)
+
+    def cross(a, b):
+        return np.array([f(a[1] * b[2]) - f(a[2] * b[1]), f(a[2] * b[0]) - f(a[0] * b[2]),
+                         f(a[0] * b[1]) - f(a[1] * b[0])], dtype=np.float32)
+
+    def normalize(a):
+        dd = f(f(f(a[0] * a[0]) + f(a[1] * a[1])) + f(a[2] * a[2]))
+        return (a / np.float32(math.sqrt(float(dd)))).astype(np.float32)
+
+    right = normalize(cross(n, pu))
+    up = normalize(cross(right, n))
+    return n, right, up
+
+
+def plane_probability_current(psi, dx, center, normal, size, sample_count, mass=1.0):
+    """Flux of the probability current through a sampled plane.
+
+    Sample point (px, py): r = c + right*dW*(px - sx/2) + up*dH*(py - sy/2), nearest
+    voxel by truncation of r/dx + N/2 (clamped to the grid here; the reference reads
+    out of bounds there), 6th-order central gradient with out-of-range neighbours
+    replaced by the centre, j.n = Im(conj(psi) dpsi/dn) / m, 2D Simpson over the samples.
+    """
+    f = np.float32
+    R = psi.real.dtype.type
+    n_arr = np.asarray(psi.shape)
+    nrm, right, up = plane_frame(normal)
+    sx, sy = int(sample_count[0]), int(sample_count[1])
+    dW = R(size[0]) / R(sx - 1)
+    dH = R(size[1]) / R(sy - 1)
+    px = (np.arange(sx) - sx // 2).astype(np.float32)
+    py = (np.arange(sy) - sy // 2).astype(np.float32)
+    c = np.asarray(center, dtype=np.float32)
+    r = np.empty((sx, sy, 3), dtype=np.float32)
+    for k in range(3):
+        # center + (right*dW)*px + (up*dH)*py, each product rounded (probability_current_density.cu:56-57)
+        a = (f(right[k] * f(dW)) * px).astype(np.float32)
+        b = (f(up[k] * f(dH)) * py).astype(np.float32)
+        r[:, :, k] = ((c[k] + a)[:, None] + b[None, :]).astype(np.float32)
+    vox = np.empty((sx, sy, 3), dtype=np.int64)
+    for k in range(3):
+        fv = r[:, :, k].astype(R) / R(dx[k]) + R(0.5) * R(n_arr[k])
+        v = np.trunc(fv).astype(np.int64)
+        vox[:, :, k] = np.clip(v, 0, n_arr[k] - 1)
+    psi_c = psi.astype(np.complex128)
+
+    def at(ix, iy, iz):
+        return psi_c[ix, iy, iz]
+
+    ix, iy, iz = vox[:, :, 0], vox[:, :, 1], vox[:, :, 2]
+    centre = at(ix, iy, iz)
+
+    def nb(axis, k):
+        idx = [ix.copy(), iy.copy(), iz.copy()]
+        moved = idx[axis] + k
+        ok = (moved >= 0) & (moved <= n_arr[axis] - 1)
+        idx[axis] = np.where(ok, moved, idx[axis])
+        return at(*idx)
+
+    grads = []
+    for axis in range(3):
+        g = (nb(axis, 3) - 9.0 * nb(axis, 2) + 45.0 * nb(axis, 1) - 45.0 * nb(axis, -1)
+             + 9.0 * nb(axis, -2) - nb(axis, -3)) / 60.0 / float(dx[axis])
+        grads.append(g)
+    dpsi = float(nrm[0]) * grads[0] + float(nrm[1]) * grads[1] + float(nrm[2]) * grads[2]
+    density = (np.conj(centre) * dpsi).imag / mass
+    wx = simpson_weights_1d(sx)
+    wy = simpson_weights_1d(sy)
+    return float(np.sum(density * wx[:, None] * wy[None, :]) / 9.0 * float(dW) * float(dH)), density

@@ -37,7 +37,7 @@ EXPORTED = [
     "wfs_batch_create", "wfs_batch_destroy", "wfs_batch_last_error", "wfs_batch_synchronize",
     "wfs_batch_init_gaussian", "wfs_batch_add_wall", "wfs_batch_add_absorbing", "wfs_batch_set_potential",
     "wfs_batch_set_psi", "wfs_batch_get_psi", "wfs_batch_run", "wfs_batch_observe", "wfs_batch_set_config",
-    "wfs_batch_autotune", "wfs_batch_launch_count", "wfs_observe_noalloc",
+    "wfs_batch_autotune", "wfs_batch_launch_count", "wfs_observe_noalloc", "wfs_plane_current",
 ]
 SCHEDULES = {"auto": 0, "axis": 1, "plane": 2}
 NPASS = 8
@@ -135,6 +135,7 @@ def load(path: str | os.PathLike | None = None):
         "wfs_batch_autotune": ([vp, dbl, dbl, i32, C.POINTER(i32), C.POINTER(i32), dp], C.c_int),
         "wfs_batch_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "wfs_observe_noalloc": ([vp, i32, C.POINTER(i32), dp, C.POINTER(Box), i32, C.POINTER(Box), dp, vp], C.c_int),
+        "wfs_plane_current": ([vp, dp, dp, dp, C.POINTER(i32), dbl, dp, vp, i32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -341,6 +342,19 @@ class Engine:
         v = C.c_int64()
         self._ck(self.lib.wfs_launch_count(self.h, C.byref(v)))
         return v.value
+
+    def plane_current(self, center, normal, size, sample_count, mass=1.0, density=False):
+        """Flux of the probability current through a plane (odd sample counts).
+        With density=True also returns the sampled current density."""
+        flux = C.c_double()
+        cnt = (C.c_int32 * 2)(int(sample_count[0]), int(sample_count[1]))
+        dens = None
+        if density:
+            dens = np.empty((int(sample_count[0]), int(sample_count[1])),
+                            dtype=np.float64 if self.double_precision else np.float32)
+        self._ck(self.lib.wfs_plane_current(self.h, _d3(center), _d3(normal), (C.c_double * 2)(*map(float, size)), cnt,
+                                            float(mass), C.byref(flux), dens.ctypes.data if dens is not None else None, 0))
+        return (flux.value, dens) if density else flux.value
 
     def norm(self) -> float:
         v = C.c_double()

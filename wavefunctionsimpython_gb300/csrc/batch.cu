@@ -639,6 +639,7 @@ int wfs_batch_autotune(wfs_batch* b, double dt, double mass, int32_t steps, int3
     std::vector<Cx<float>> saved(b->total);
     int rc = materialize(b);
     if (rc) return rc;
+    BCK(cudaStreamSynchronize(b->stream));
     BCK(cudaMemcpy(saved.data(), b->psi, b->total * sizeof(Cx<float>), cudaMemcpyDeviceToHost));
     const int cls[5] = {1, 2, 4, 8, 16};
     double best = 1e30;
@@ -673,6 +674,7 @@ int wfs_batch_autotune(wfs_batch* b, double dt, double mass, int32_t steps, int3
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
+    BCK(cudaStreamSynchronize(b->stream));  // the last timed configuration may still be running
     BCK(cudaMemcpy(b->psi, saved.data(), b->total * sizeof(Cx<float>), cudaMemcpyHostToDevice));
     b->rep = 0;
     b->cluster = bc;

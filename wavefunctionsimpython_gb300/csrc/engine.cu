@@ -23,6 +23,7 @@
 #include "../../include/wfs.h"
 #include "kernels.h"
 #include "plane_kernels.cuh"
+#include "host_helpers.h"
 
 using namespace wfs;
 
@@ -313,6 +314,10 @@ int to_real(wfs_handle* h) {
 }
 
 bool fft_ready(wfs_handle* h) {
+    if (h->count >= (int64_t(1) << 31)) {  // the pass kernels index psi with 32-bit element offsets
+        set_err(h, WFS_ERR_UNSUPPORTED, "split-step: grids of 2^31 sites or more are not supported");
+        return false;
+    }
     for (int a = 0; a < 3; ++a)
         if (!fft_length_supported(h->n[a], is_dbl(h))) {
             set_err(h, WFS_ERR_UNSUPPORTED, "split-step: axis length " + std::to_string(h->n[a]) +
@@ -962,6 +967,54 @@ int wfs_launch_count(wfs_handle* h, int64_t* out) {
     if (!h) return dispatch_err(h);
     if (!out) return set_err(h, WFS_ERR_ARG, "null output");
     *out = h->launches;
+    return WFS_OK;
+}
+
+int wfs_plane_current(wfs_handle* h, const double center[3], const double normal[3], const double size[2],
+                      const int32_t count[2], double mass, double* flux_out, void* density_out, int32_t to_device) {
+    if (!h) return dispatch_err(h);
+    if (!center || !normal || !size || !count || !flux_out || !(mass > 0)) return set_err(h, WFS_ERR_ARG, "invalid argument");
+    if (count[0] < 3 || count[1] < 3 || (count[0] % 2) == 0 || (count[1] % 2) == 0)
+        return set_err(h, WFS_ERR_ARG, "sample counts must be odd and >= 3 (Simpson)");
+    PlaneCurrentArgs a;
+    std::memset(&a, 0, sizeof(a));
+    if (!plane_frame(normal, a.normal, a.right, a.up)) return set_err(h, WFS_ERR_ARG, "degenerate plane normal");
+    for (int k = 0; k < 3; ++k) {
+        a.n[k] = h->n[k];
+        a.dx[k] = h->dx[k];
+        a.center[k] = float(center[k]);
+    }
+    a.sx = count[0];
+    a.sy = count[1];
+    a.mass = mass;
+    const double dW = is_dbl(h) ? size[0] / double(a.sx - 1) : double(float(size[0]) / float(a.sx - 1));
+    const double dH = is_dbl(h) ? size[1] / double(a.sy - 1) : double(float(size[1]) / float(a.sy - 1));
+    a.dWf = float(dW);
+    a.dHf = float(dH);
+    int rc = is_dbl(h) ? to_real<double>(h) : to_real<float>(h);
+    if (rc) return rc;
+    const int max_blocks = 1024;
+    if ((rc = ensure_partials(h, max_blocks))) return rc;
+    const size_t dbytes = size_t(a.sx) * a.sy * (is_dbl(h) ? sizeof(double) : sizeof(float));
+    void* dens = nullptr;
+    if (density_out) {
+        if (to_device) dens = density_out;
+        else CK(cudaMalloc(&dens, dbytes));
+    }
+    int grid = 0;
+    cudaError_t e;
+    {
+        PassScope ps(h, WFS_PASS_OBSERVE);
+        e = is_dbl(h) ? launch_plane_current<double>((const Cx<double>*)h->psi, a, h->partials, max_blocks, (double*)dens, h->stream, &grid)
+                      : launch_plane_current<float>((const Cx<float>*)h->psi, a, h->partials, max_blocks, (float*)dens, h->stream, &grid);
+    }
+    if (e == cudaSuccess) e = launch_reduce_partials(h->partials, grid, 1, h->dres, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->hres, h->dres, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && density_out && !to_device) e = cudaMemcpyAsync(density_out, dens, dbytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (density_out && !to_device && dens) cudaFree(dens);
+    if (e != cudaSuccess) return set_err(h, WFS_ERR_CUDA, std::string("plane current: ") + cudaGetErrorString(e));
+    *flux_out = h->hres[0] * dW * dH / 9.0;
     return WFS_OK;
 }
 

@@ -54,15 +54,17 @@ __device__ __forceinline__ R simpson_w(int v, int b, int cnt) {
 }
 
 // Block-wide sum of acc[0..nq) written to partials[blockIdx.x * nq + q].
-template <int NQ>
-__device__ __forceinline__ void block_reduce_store(double (&acc)[NQ], int nq, double* scratch, double* out) {
+// Warp sums use the working precision R (a 32-term tree); the sums of the warps
+// and, later, of the blocks are FP64. FP64 work is a few adds per block.
+template <int NQ, typename R>
+__device__ __forceinline__ void block_reduce_store(R (&acc)[NQ], int nq, double* scratch, double* out) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-        double v = acc[q];
+        R v = acc[q];
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if (lane == 0 && q < nq) scratch[q * 32 + warp] = v;
+        if (lane == 0 && q < nq) scratch[q * 32 + warp] = double(v);
     }
     __syncthreads();
     if (threadIdx.x < nq) {
@@ -72,11 +74,12 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[NQ], int nq, do
     }
 }
 
-// Observation sums. A thread first sums the few elements of one (x, y) row it
-// holds in the working precision (RowAcc: Simpson z-weight * |psi|^2 per box,
-// and the location moments in z), then folds the row into FP64 sums with the
-// row's x/y weights (obs_row_flush). FP64 work is thus per row and per thread,
-// not per element: GB300's FP64 rate is a small fraction of its FP32 rate.
+// Observation sums. A thread sums the few elements of one (x, y) row it holds
+// (RowAcc: Simpson z-weight * |psi|^2 per box, and the location moments in z),
+// folds the row in with the row's x/y weights (obs_row_flush), and the block
+// reduction adds threads in a 32-term tree; all of that is in the working
+// precision. Only warp-to-block and block-to-grid sums are FP64, since GB300's
+// FP64 rate is a small fraction of its FP32 rate.
 template <typename R>
 struct RowAcc {
     R box[kMaxBox];
@@ -104,20 +107,20 @@ __device__ __forceinline__ void obs_row_element(const ObsArgs& o, RowAcc<R>& ra,
 }
 
 template <typename R>
-__device__ __forceinline__ void obs_row_flush(const ObsArgs& o, double (&acc)[kMaxBox + kLocQ], const RowAcc<R>& ra,
+__device__ __forceinline__ void obs_row_flush(const ObsArgs& o, R (&acc)[kMaxBox + kLocQ], const RowAcc<R>& ra,
                                               const R (&wxy)[kMaxBox], R lxy, R rx, R ry) {
 #pragma unroll
     for (int b = 0; b < kMaxBox; ++b)
-        if (b < o.nbox) acc[b] += double(wxy[b]) * double(ra.box[b]);
+        if (b < o.nbox) acc[b] += wxy[b] * ra.box[b];
     if (o.has_loc && lxy != R(0)) {
-        const double l = double(lxy), s0 = double(ra.s0), x = double(rx), y = double(ry);
-        acc[kMaxBox + 0] += l * s0;
-        acc[kMaxBox + 1] += l * x * s0;
-        acc[kMaxBox + 2] += l * y * s0;
-        acc[kMaxBox + 3] += l * double(ra.sz);
-        acc[kMaxBox + 4] += l * x * x * s0;
-        acc[kMaxBox + 5] += l * y * y * s0;
-        acc[kMaxBox + 6] += l * double(ra.szz);
+        const R ls0 = lxy * ra.s0;
+        acc[kMaxBox + 0] += ls0;
+        acc[kMaxBox + 1] += rx * ls0;
+        acc[kMaxBox + 2] += ry * ls0;
+        acc[kMaxBox + 3] += lxy * ra.sz;
+        acc[kMaxBox + 4] += rx * rx * ls0;
+        acc[kMaxBox + 5] += ry * ry * ls0;
+        acc[kMaxBox + 6] += lxy * ra.szz;
     }
 }
 
@@ -140,10 +143,11 @@ __device__ __forceinline__ void obs_row_factors(const ObsArgs& o, int x, int y, 
 }
 
 // Compacts the fixed accumulator layout to [nbox probs][loc sums] and stores per-CTA partials.
-__device__ __forceinline__ void obs_store(const ObsArgs& o, double (&acc)[kMaxBox + kLocQ], double* scratch) {
-    double packed[kMaxBox + kLocQ];
+template <typename R>
+__device__ __forceinline__ void obs_store(const ObsArgs& o, R (&acc)[kMaxBox + kLocQ], double* scratch) {
+    R packed[kMaxBox + kLocQ];
 #pragma unroll
-    for (int q = 0; q < kMaxBox + kLocQ; ++q) packed[q] = 0.0;
+    for (int q = 0; q < kMaxBox + kLocQ; ++q) packed[q] = R(0);
 #pragma unroll
     for (int b = 0; b < kMaxBox; ++b)
         if (b < o.nbox) packed[b] = acc[b];
@@ -161,7 +165,7 @@ __device__ __forceinline__ void obs_store(const ObsArgs& o, double (&acc)[kMaxBo
 // Strided pass (x or y axis)
 // ---------------------------------------------------------------------------
 template <typename R, int P, int Q, int W, int OP>
-__global__ void __launch_bounds__(cmax(P, Q) * W) fft_strided_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_strided_kernel(const PassArgs<R> a) {
     constexpr int L = P * Q;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Cx<R>* sm = reinterpret_cast<Cx<R>*>(smem_raw);
@@ -171,12 +175,14 @@ __global__ void __launch_bounds__(cmax(P, Q) * W) fft_strided_kernel(const PassA
     const int col = tile * W + c;
     const bool active = col < a.ncols;
     Cx<R>* base = a.data + outer * a.outer_stride + col;
-    const int64_t rs = a.row_stride;
+    // 32-bit element offsets from one 64-bit base (the host guarantees L * row_stride < 2^31);
+    // 64-bit per-row addresses kept live from load to store cost 32 registers
+    const int rs = int(a.row_stride);
 
     Cx<R> a1[Q], a2[P];
     if (t < P) {
 #pragma unroll
-        for (int i = 0; i < Q; ++i) a1[i] = active ? base[(int64_t)(t + P * i) * rs] : mk<R>(R(0), R(0));
+        for (int i = 0; i < Q; ++i) a1[i] = active ? base[(t + P * i) * rs] : mk<R>(R(0), R(0));
     }
     auto sidx_f = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
     auto sidx_i = [&](int k2, int n1) { return (k2 * Q + n1) * W + c; };
@@ -186,7 +192,7 @@ __global__ void __launch_bounds__(cmax(P, Q) * W) fft_strided_kernel(const PassA
         else two_stage<P, Q, +1, R>(a1, a2, sm, a.tw, t, sidx_f);
         if (active && t < Q) {
 #pragma unroll
-            for (int k = 0; k < P; ++k) base[(int64_t)(t + Q * k) * rs] = scale(a2[k], a.scale);
+            for (int k = 0; k < P; ++k) base[(t + Q * k) * rs] = scale(a2[k], a.scale);
         }
     } else {  // OP_KIN: forward, diagonal kinetic factor, inverse
         two_stage<P, Q, -1, R>(a1, a2, sm, a.tw, t, sidx_f);
@@ -200,7 +206,7 @@ __global__ void __launch_bounds__(cmax(P, Q) * W) fft_strided_kernel(const PassA
         two_stage<Q, P, +1, R>(a2, a1, sm, a.tw, t, sidx_i);
         if (active && t < P) {
 #pragma unroll
-            for (int i = 0; i < Q; ++i) base[(int64_t)(t + P * i) * rs] = a1[i];
+            for (int i = 0; i < Q; ++i) base[(t + P * i) * rs] = a1[i];
         }
     }
 }
@@ -209,7 +215,7 @@ __global__ void __launch_bounds__(cmax(P, Q) * W) fft_strided_kernel(const PassA
 // Contiguous pass (z axis)
 // ---------------------------------------------------------------------------
 template <typename R, int P, int Q, int W, int OP>
-__global__ void __launch_bounds__(cmax(P, Q) * W) fft_contig_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_contig_kernel(const PassArgs<R> a) {
     constexpr int L = P * Q, T = cmax(P, Q);
     constexpr int RS = cmax(Q * (P + 1), P * (Q + 1));
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -252,9 +258,9 @@ __global__ void __launch_bounds__(cmax(P, Q) * W) fft_contig_kernel(const PassAr
         }
     } else {  // OP_OBS: inverse transform in registers, observe, no store
         two_stage<P, Q, +1, R>(a1, a2, sm, a.tw, t, sidx_f);
-        double acc[kMaxBox + kLocQ];
+        R acc[kMaxBox + kLocQ];
 #pragma unroll
-        for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = 0.0;
+        for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = R(0);
         if (active && t < Q) {
             const ObsArgs& o = a.obs;
             const int x = int(row / o.n[1]), y = int(row % o.n[1]);

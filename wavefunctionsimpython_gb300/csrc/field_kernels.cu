@@ -365,9 +365,9 @@ __global__ void __launch_bounds__(256) observe_real_kernel(const Cx<R>* __restri
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t nrows = int64_t(o.n[0]) * o.n[1];
     const int64_t row = int64_t(blockIdx.x) * kObsRowsPerCta + warp;
-    double acc[kMaxBox + kLocQ];
+    R acc[kMaxBox + kLocQ];
 #pragma unroll
-    for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = 0.0;
+    for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = R(0);
     if (row < nrows) {
         const int x = int(row / o.n[1]), y = int(row % o.n[1]);
         R wxy[kMaxBox], lxy, rx, ry;
@@ -416,15 +416,16 @@ cudaError_t launch_reduce_partials(const double* partials, int nblocks, int nq, 
 template <typename R>
 __global__ void __launch_bounds__(256) norm_kernel(const Cx<R>* __restrict__ psi, int64_t count, double* partials, int* flag) {
     __shared__ double scratch[32];
-    double s = 0.0;
+    R st = R(0);  // per-thread sum in the working precision (a few dozen terms)
     bool bad = false;
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
         Cx<R> v = psi[i];
-        double p = double(v.x) * double(v.x) + double(v.y) * double(v.y);
+        R p = v.x * v.x + v.y * v.y;
         if (!isfinite(p)) bad = true;
-        s += p;
+        st += p;
     }
     if (bad) atomicExch(flag, 1);
+    double s = double(st);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     if (lane == 0) scratch[warp] = s;

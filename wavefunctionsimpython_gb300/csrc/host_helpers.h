@@ -98,6 +98,36 @@ inline bool wall_frame(const wfs_wall* w, WallDev& wd) {
     return true;
 }
 
+// Frame of a sampling plane (probability_current_density.cu:41-49), float32 with
+// every product and sum rounded: prefUp = (0,1,0), or (0,0,1) when |n.y| > 0.99;
+// right = normalize(n x prefUp); up = normalize(right x n).
+inline bool plane_frame(const double normal[3], float n[3], float right[3], float up[3]) {
+    const double nn = std::sqrt(normal[0] * normal[0] + normal[1] * normal[1] + normal[2] * normal[2]);
+    if (!(nn > 0)) return false;
+    auto mul = [](float a, float b) { volatile float r = a * b; return float(r); };
+    auto add = [](float a, float b) { volatile float r = a + b; return float(r); };
+    auto sub = [](float a, float b) { volatile float r = a - b; return float(r); };
+    for (int i = 0; i < 3; ++i) n[i] = float(normal[i] / nn);
+    float pu[3] = {0.f, 1.f, 0.f};
+    if (std::fabs(add(add(mul(n[0], pu[0]), mul(n[1], pu[1])), mul(n[2], pu[2]))) > 0.99f) { pu[1] = 0.f; pu[2] = 1.f; }
+    auto cross = [&](const float* a, const float* b, float* o) {
+        o[0] = sub(mul(a[1], b[2]), mul(a[2], b[1]));
+        o[1] = sub(mul(a[2], b[0]), mul(a[0], b[2]));
+        o[2] = sub(mul(a[0], b[1]), mul(a[1], b[0]));
+    };
+    auto normalize = [&](float* a) -> bool {
+        const float d = add(add(mul(a[0], a[0]), mul(a[1], a[1])), mul(a[2], a[2]));
+        const float l = float(std::sqrt(double(d)));
+        if (!(l > 0)) return false;
+        for (int i = 0; i < 3; ++i) { volatile float r = a[i] / l; a[i] = r; }
+        return true;
+    };
+    cross(n, pu, right);
+    if (!normalize(right)) return false;
+    cross(right, n, up);
+    return normalize(up);
+}
+
 inline AbsorbDev absorbing_dev(const wfs_absorbing* a) {
     AbsorbDev ad;
     for (int i = 0; i < 3; ++i) {

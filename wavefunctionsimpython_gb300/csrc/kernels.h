@@ -7,6 +7,17 @@
 
 #include "common.cuh"
 
+// Resident blocks per SM the FFT pass kernels and the fused plane kernel are
+// register-budgeted for (build-time tuning knobs). Measured at 256^3 complex64
+// on GB300: 2 for the pass kernels (x pass 75 us vs 84 us at 3) and 3 for the
+// plane kernel (162 us vs 175 us at 2 and 258 us unconstrained).
+#ifndef WFS_MINB_PASS
+#define WFS_MINB_PASS 2
+#endif
+#ifndef WFS_MINB_PLANE
+#define WFS_MINB_PLANE 3
+#endif
+
 namespace wfs {
 
 constexpr int kMaxBox = 8;      // volume-probability boxes per fused observation
@@ -99,6 +110,19 @@ cudaError_t launch_observe_real(const Cx<R>* psi, const ObsArgs& o, cudaStream_t
 cudaError_t launch_reduce_partials(const double* partials, int nblocks, int nq, double* out, cudaStream_t s);
 template <typename R>
 cudaError_t launch_norm(const Cx<R>* psi, int64_t count, double* partials, int* nblocks, int* flag, cudaStream_t s);
+
+// ---- plane probability current (current.cu) ----
+struct PlaneCurrentArgs {
+    int n[3];
+    double dx[3];
+    float center[3], right[3], up[3], normal[3];  // float32 frame, as the reference computes it
+    float dWf, dHf;                                 // sample spacings on the plane
+    int sx, sy;                                     // odd sample counts
+    double mass;
+};
+template <typename R>
+cudaError_t launch_plane_current(const Cx<R>* psi, const PlaneCurrentArgs& a, double* partials, int max_blocks,
+                                 R* density, cudaStream_t s, int* grid_out);
 
 // ---- power series (taylor.cu) ----
 template <typename R>

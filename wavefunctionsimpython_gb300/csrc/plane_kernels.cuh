@@ -125,7 +125,7 @@ __device__ __forceinline__ void plane_z_tile(Cx<R>* plane, const Cx<R>* eplane, 
 }
 
 template <typename R, int LY, int LZ, int CL, int NT>
-__global__ void __launch_bounds__(NT) plane_step_kernel(const PlaneArgs<R> a) {
+__global__ void __launch_bounds__(NT, WFS_MINB_PLANE) plane_step_kernel(const PlaneArgs<R> a) {
     constexpr int PY = PlanOf<LY>::P, QY = PlanOf<LY>::Q, TY = cmax(PY, QY);
     constexpr int PZ = PlanOf<LZ>::P, QZ = PlanOf<LZ>::Q, TZ = cmax(PZ, QZ);
     constexpr int WY = StridedW<R, TY>::value;
