@@ -1,4 +1,4 @@
-"""The C-ABI library loads and exports every entry point include/wfs.h declares (CPU only)."""
+"""The C-ABI library loads and exports every entry point include/*.h declares (CPU only)."""
 import re
 import shutil
 from pathlib import Path
@@ -8,15 +8,20 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 
 
-def declared_symbols():
-    text = (ROOT / "include" / "wfs.h").read_text()
-    return sorted(set(re.findall(r"^(?:int|const char\*)\s+(wfs_\w+)\s*\(", text, flags=re.M)))
+def declared_symbols(header="wfs.h"):
+    text = (ROOT / "include" / header).read_text()
+    return sorted(set(re.findall(r"^(?:int|int64_t|const char\*)\s+(wfs_\w+)\s*\(", text, flags=re.M)))
+
+
+def all_declared_symbols():
+    return sorted(s for h in sorted(p.name for p in (ROOT / "include").glob("*.h")) for s in declared_symbols(h))
 
 
 def test_header_matches_binding_list():
     from wavefunctionsimpython_gb300 import _lib
 
-    assert declared_symbols() == sorted(_lib.EXPORTED)
+    assert declared_symbols("wfs.h") == sorted(_lib.EXPORTED)
+    assert declared_symbols("wfs_fno.h") == sorted(_lib.FNO_EXPORTED)
 
 
 def test_library_exports_every_declared_symbol():
@@ -26,7 +31,7 @@ def test_library_exports_every_declared_symbol():
 
     build_ext.build()
     lib = _lib.load()
-    for name in declared_symbols():
+    for name in all_declared_symbols():
         assert hasattr(lib, name), name
     assert lib.wfs_abi_version() == 1
 

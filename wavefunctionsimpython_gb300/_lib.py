@@ -39,6 +39,13 @@ EXPORTED = [
     "wfs_batch_set_psi", "wfs_batch_get_psi", "wfs_batch_run", "wfs_batch_observe", "wfs_batch_set_config",
     "wfs_batch_autotune", "wfs_batch_launch_count", "wfs_observe_noalloc", "wfs_plane_current",
 ]
+# Every entry point include/wfs_fno.h declares (the surrogate's kernels).
+FNO_EXPORTED = [
+    "wfs_fno_pointwise", "wfs_fno_pointwise_backward", "wfs_fno_wgrad_scratch", "wfs_fno_weight_grad",
+    "wfs_fno_fft3", "wfs_fno_gather", "wfs_fno_scatter", "wfs_fno_pack_weights", "wfs_fno_mix",
+    "wfs_fno_spectral_weight_grad", "wfs_fno_adam", "wfs_fno_loss", "wfs_fno_sample_norms",
+    "wfs_fno_make_input", "wfs_fno_scale_samples",
+]
 SCHEDULES = {"auto": 0, "axis": 1, "plane": 2}
 NPASS = 8
 PASS_NAMES = ["x_kin", "y", "z_vph", "z", "observe", "taylor", "other", "plane"]
@@ -89,7 +96,7 @@ def load(path: str | os.PathLike | None = None):
     if not p.exists():
         raise ImportError(f"{p} is missing: build it with wavefunctionsimpython_gb300.build_ext.build()")
     lib = C.CDLL(str(p))
-    vp, i32, dbl = C.c_void_p, C.c_int32, C.c_double
+    vp, i32, dbl, i64 = C.c_void_p, C.c_int32, C.c_double, C.c_int64
     dp = C.POINTER(C.c_double)
     sig = {
         "wfs_abi_version": ([], C.c_int),
@@ -136,6 +143,23 @@ def load(path: str | os.PathLike | None = None):
         "wfs_batch_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "wfs_observe_noalloc": ([vp, i32, C.POINTER(i32), dp, C.POINTER(Box), i32, C.POINTER(Box), dp, vp], C.c_int),
         "wfs_plane_current": ([vp, dp, dp, dp, C.POINTER(i32), dbl, dp, vp, i32], C.c_int),
+        # surrogate kernels (include/wfs_fno.h); every pointer is a device pointer
+        "wfs_fno_pointwise": ([vp, i32, vp, vp, vp, vp, vp, vp, i32, i32, i64, i32, vp], C.c_int),
+        "wfs_fno_pointwise_backward": ([vp, vp, vp, i32, vp, vp, vp, i32, i32, i32, i64, vp], C.c_int),
+        "wfs_fno_wgrad_scratch": ([i32, i32], C.c_int64),
+        "wfs_fno_weight_grad": ([vp, i32, vp, i32, i32, i64, vp, vp, vp], C.c_int),
+        "wfs_fno_fft3": ([vp, i64, i32, i32, vp], C.c_int),
+        "wfs_fno_gather": ([vp, vp, i32, i32, i32, i32, vp], C.c_int),
+        "wfs_fno_scatter": ([vp, vp, i32, i32, i32, i32, vp], C.c_int),
+        "wfs_fno_pack_weights": ([vp, vp, vp, i32, i32, vp], C.c_int),
+        "wfs_fno_mix": ([vp, vp, vp, i32, i32, i32, vp], C.c_int),
+        "wfs_fno_spectral_weight_grad": ([vp, vp, vp, i32, i32, i32, vp], C.c_int),
+        "wfs_fno_adam": ([vp, vp, vp, vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp],
+                         C.c_int),
+        "wfs_fno_loss": ([vp, vp, i64, i32, vp, vp, vp, vp], C.c_int),
+        "wfs_fno_sample_norms": ([vp, vp, i64, i32, vp, vp, vp], C.c_int),
+        "wfs_fno_make_input": ([vp, vp, C.c_float, vp, vp, i32, i64, vp], C.c_int),
+        "wfs_fno_scale_samples": ([vp, vp, i32, i32, i64, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -427,6 +451,16 @@ class Batch:
         out = np.empty((L, L, L), dtype=np.complex64)
         self._ck(self.lib.wfs_batch_get_psi(self.h, int(i), out.ctypes.data, 0))
         return out
+
+    # device-pointer variants (complex64 L^3 buffers already on this batch's GPU)
+    def set_psi_device(self, i, ptr):
+        self._ck(self.lib.wfs_batch_set_psi(self.h, int(i), int(ptr), 1))
+
+    def get_psi_device(self, i, ptr):
+        self._ck(self.lib.wfs_batch_get_psi(self.h, int(i), int(ptr), 1))
+
+    def set_potential_device(self, i, ptr):
+        self._ck(self.lib.wfs_batch_set_potential(self.h, int(i), int(ptr), 1))
 
     def run(self, nsteps, dt, mass=1.0, graph=True):
         self._ck(self.lib.wfs_batch_run(self.h, int(nsteps), float(dt), float(mass), 1 if graph else 0))
