@@ -431,6 +431,167 @@ def run_batch(args):
     return 0
 
 
+def run_surrogate(args):
+    """FNO surrogate (64^3, width 32, 12 modes, 4 layers, BF16 spectral mixing): trains on
+    pairs from the plain split step, then measures held-out jumps of K = 50 steps against
+    the exact propagator, the acceptance rate at the 1e-2 tolerance, and the effective
+    speedup plain / (surrogate + rejected * plain + verified * plain)."""
+    import ctypes
+
+    import torch
+    from wavefunctionsimpython_gb300 import fno as F
+
+    torch.cuda.set_device(args.device)
+    stream = engine_stream(torch)
+    if args.fno_dist == "inband":
+        # oscillators whose packets stay inside the 12 kept modes of a 24-Bohr box
+        cfg = F.FnoConfig(extent=24.0, prior_steps=1)
+        ranges = F.ScenarioRanges(p_wall=0.0, p_ho=1.0, omega=(0.2, 0.8), sigma=(1.0, 2.0), x0=(-3.0, -1.0),
+                                  k0=(0.2, 1.0))
+    else:
+        cfg = F.FnoConfig(extent=40.0, prior_steps=2)
+        ranges = F.ScenarioRanges()
+    G, W, B = 64, 8, 8
+    tol, verify_frac = 1e-2, 1.0 / 16
+    chunk = G * W * 5
+    nchunks = max(1, args.fno_pairs // chunk)
+    model = F.FNO(cfg, seed=0, stream=stream)
+    gen = F.PairGenerator(cfg, G, stream=stream)
+    t_gen = t_train = 0.0
+    # time a few training steps to turn the time budget into a step count
+    t0 = time.perf_counter()
+    data = F.make_dataset(cfg, chunk, W, G, seed=100, stream=stream, gen=gen, ranges=ranges)
+    stream.synchronize()
+    t_gen += time.perf_counter() - t0
+    probe = F.FNO(cfg, seed=1, stream=stream)
+    F.train(probe, data[:3], B, 5, 1e-4)
+    t_probe = F.train(probe, data[:3], B, 20, 1e-4)["seconds"] / 20
+    del probe
+    total_steps = max(nchunks, int(args.fno_train_seconds / t_probe))
+    per_chunk = total_steps // nchunks
+    history, done = [], 0
+    for c in range(nchunks):
+        if c > 0:
+            del data
+            t0 = time.perf_counter()
+            data = F.make_dataset(cfg, chunk, W, G, seed=100 + c, stream=stream, gen=gen, ranges=ranges)
+            stream.synchronize()
+            t_gen += time.perf_counter() - t0
+        info = F.train(model, data[:3], B, per_chunk, args.fno_lr, warmup=200, log_every=max(1, per_chunk // 4),
+                       seed=c, step_offset=done, total_steps=per_chunk * nchunks)
+        done += info["steps"]
+        t_train += info["seconds"]
+        history += info["history"]
+    del data
+    torch.cuda.empty_cache()
+
+    # held-out seeds: one random window per scenario
+    rng = np.random.default_rng(777)
+    e_net, e_prior, n_err, kinds = [], [], [], []
+    for g in range(args.fno_eval // G):
+        held = F.make_dataset(cfg, G * W, W, G, seed=10_000 + g, stream=stream, gen=gen, ranges=ranges)
+        rows = torch.tensor([int(rng.integers(W)) * G + i for i in range(G)], device=held[0].device)
+        sel = tuple(torch.index_select(t, 0, rows) for t in held[:3])
+        ev = F.evaluate(model, sel, batch=16)
+        e_net.append(ev["err_net"])
+        e_prior.append(ev["err_prior"])
+        n_err.append(ev["norm_err_net"])
+        kinds += [held[4][r].kind for r in rows.tolist()]
+        del held, sel
+    e_net, e_prior, n_err = np.concatenate(e_net), np.concatenate(e_prior), np.concatenate(n_err)
+    acc_net = (e_net <= tol) & (n_err <= tol)
+    acc_prior = e_prior <= tol
+
+    # cost of one jump per sample: plain (K exact steps) vs surrogate (coarse step + network)
+    gen.setup(F.draw_scenarios(G, np.random.default_rng(5), ranges))
+    T = cfg.jump_steps * cfg.dt
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        fn()
+        stream.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        stream.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    ms_plain = timed(lambda: gen.exact.run(cfg.jump_steps, cfg.dt, cfg.mass, graph=True), 5) / G
+    ms_coarse = timed(lambda: gen.coarse.run(max(1, cfg.prior_steps), T / max(1, cfg.prior_steps), cfg.mass,
+                                             graph=True), 10) / G if cfg.prior_steps else 0.0
+    x = torch.zeros((G, 2, cfg.n3), dtype=torch.complex64, device=stream.device)
+    psi = torch.zeros((G, cfg.n3), dtype=torch.complex64, device=stream.device)
+    gen.snapshot(psi)
+    prior = psi.clone()
+    a2 = torch.empty(G, dtype=torch.float64, device=stream.device)
+    lib = model.lib
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    out = torch.empty_like(prior)
+    IB = 16
+
+    def infer():
+        lib.wfs_fno_sample_norms(F._ptr(psi), None, cfg.n3, G, F._ptr(a2), None, sp)
+        lib.wfs_fno_make_input(F._ptr(psi), F._ptr(gen.V), float(cfg.vscale), F._ptr(a2), F._ptr(x), G, cfg.n3, sp)
+        lib.wfs_fno_scale_samples(F._ptr(prior), F._ptr(a2), 1, G, cfg.n3, sp)
+        for k in range(0, G, IB):
+            model.forward(x[k:k + IB], prior[k:k + IB], IB, out=out[k:k + IB])
+        lib.wfs_fno_scale_samples(F._ptr(out), F._ptr(a2), 0, G, cfg.n3, sp)
+        lib.wfs_fno_sample_norms(F._ptr(out), None, cfg.n3, G, F._ptr(a2), None, sp)
+
+    ms_net = timed(infer, 5) / G
+    rej_net, rej_prior = 1.0 - acc_net.mean(), 1.0 - acc_prior.mean()
+    ms_surr = ms_coarse + ms_net
+    speed_net = ms_plain / (ms_surr + (rej_net + verify_frac) * ms_plain)
+    speed_prior = ms_plain / (ms_coarse + (rej_prior + verify_frac) * ms_plain)
+    peak, peak_kind = load_peaks()
+    nm = cfg.nmodes
+    mix_flops = 2 * 4 * nm * cfg.width * cfg.width * 2 * cfg.layers  # fwd, per sample: 4 real MACs per complex
+    line = {"metric": "FNO surrogate effective speedup vs plain split step (K=50 jumps, 64^3 c64)",
+            "value": speed_net, "unit": "x", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 spectral mixing / f32", "data": "synthetic",
+            "config": {"workload": f"FNO 64^3 width {cfg.width} modes {cfg.modes} layers {cfg.layers}, "
+                                   f"K={cfg.jump_steps}, prior {cfg.prior_steps} coarse steps",
+                       "distribution": args.fno_dist, "extent": cfg.extent, "ranges": ranges.__dict__,
+                       "train_pairs": nchunks * chunk, "batch": B, "lr": args.fno_lr},
+            "training": {"steps": done, "samples_seen": done * B, "seconds": t_train, "gen_seconds": t_gen,
+                         "ms_per_step": 1e3 * t_train / max(1, done), "loss_history": history[-12:]},
+            "held_out": {"seeds": int(e_net.size), "err_net_mean": float(e_net.mean()),
+                         "err_net_median": float(np.median(e_net)), "err_prior_mean": float(e_prior.mean()),
+                         "err_prior_median": float(np.median(e_prior)), "norm_err_net_max": float(n_err.max()),
+                         "accept_net": float(acc_net.mean()), "accept_prior_only": float(acc_prior.mean())},
+            "ms_per_jump_per_sample": {"plain": ms_plain, "coarse_prior": ms_coarse, "network": ms_net},
+            "effective_speedup": {"surrogate": speed_net, "coarse_prior_only": speed_prior,
+                                  "verify_fraction": verify_frac, "tolerance": tol},
+            "network_only_site_jumps_per_s": cfg.n3 / (ms_net * 1e-3),
+            "spectral_mixing": {"tflops_fwd": mix_flops / (ms_net * 1e-3) / 1e12,
+                                "note": "the mixing is a small share of the network's time; see ms_per_jump"}}
+    if not args.no_cpu_baseline:
+        # FP64 NumPy oracle for two held-out jumps: accuracy of the exact engine and of the surrogate
+        from oracle import wfs_oracle as orc
+
+        held = F.make_dataset(cfg, G, 1, G, seed=20_000, stream=stream, gen=gen, ranges=ranges)
+        pred = model.forward(held[0][:2], held[1][:2], 2).cpu().numpy()
+        xs, tg = held[0][:2].cpu().numpy(), held[2][:2].cpu().numpy()
+        n3 = (cfg.N,) * 3
+        dx = orc.delta_x((cfg.extent,) * 3, n3)
+        t0 = time.perf_counter()
+        errs = []
+        for i in range(2):
+            V = gen._potential(held[4][i]).astype(np.complex128)
+            ex = orc.split_step(xs[i, 0].astype(np.complex128).reshape(n3), V, dx, cfg.dt, cfg.mass,
+                                nsteps=cfg.jump_steps)
+            nrm = np.linalg.norm(ex)
+            errs.append({"engine_vs_fp64": float(np.linalg.norm(tg[i].reshape(n3) - ex) / nrm),
+                         "surrogate_vs_fp64": float(np.linalg.norm(pred[i].reshape(n3) - ex) / nrm)})
+        dt_cpu = (time.perf_counter() - t0) / 2
+        line["fp64_oracle_check"] = errs
+        line["cpu_baseline"] = {"value": 1.0 / dt_cpu, "unit": "jumps/s", "cores": 1, "kind": "port",
+                                "sample": "2 held-out K=50 jumps of the FP64 NumPy split step (pocketfft, 1 thread)"}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -441,9 +602,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", choices=["auto", "axis", "plane"], default="auto",
                     help="split-step schedule: fused yz-plane pass (auto) or one pass per axis")
-    ap.add_argument("--workload", choices=["split", "taylor", "batch"], default="split",
+    ap.add_argument("--workload", choices=["split", "taylor", "batch", "surrogate"], default="split",
                     help="split: the headline 256^3 double slit; taylor: the 128^3 power-series workload; "
-                         "batch: the 256-instance uneven sweep")
+                         "batch: the 256-instance uneven sweep; surrogate: train and measure the FNO jump")
+    ap.add_argument("--fno-dist", choices=["inband", "sweep"], default="inband",
+                    help="surrogate scenarios: oscillators inside the kept modes, or the sweep's barriers and "
+                         "oscillators on a 40-Bohr box")
+    ap.add_argument("--fno-train-seconds", type=float, default=240.0)
+    ap.add_argument("--fno-pairs", type=int, default=20480)
+    ap.add_argument("--fno-eval", type=int, default=2048)
+    ap.add_argument("--fno-lr", type=float, default=1e-3)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -453,6 +621,8 @@ def main():
         return run_taylor(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "surrogate":
+        return run_surrogate(args)
     return run_own(args)
 
 

@@ -85,10 +85,12 @@ int wfs_fno_adam(float* p, const float* g, float* m1, float* m2, int64_t n, floa
                  float eps, float weight_decay, int32_t step, void* stream);
 
 /* Per-sample relative squared error e_b = |pred_b - target_b|^2 / |target_b|^2
- * (per_sample floats each), loss = mean_b e_b, grad = d loss / d pred (may be NULL).
+ * (per_sample floats each), loss = mean_b e_b, grad = grad_scale * d loss / d pred
+ * (may be NULL). A grad_scale of per_sample trains on the per-element relative
+ * error, whose gradients stay well above the optimiser's epsilon.
  * sample_err[B] and loss[1] are device floats. */
-int wfs_fno_loss(const float* pred, const float* target, int64_t per_sample, int32_t B, float* sample_err,
-                 float* grad, float* loss, void* stream);
+int wfs_fno_loss(const float* pred, const float* target, int64_t per_sample, int32_t B, float grad_scale,
+                 float* sample_err, float* grad, float* loss, void* stream);
 
 /* Per-sample |a_b|^2 and |a_b - c_b|^2 in FP64 (acceptance test of a jump). */
 int wfs_fno_sample_norms(const void* a, const void* c, int64_t per_sample, int32_t B, double* a2, double* d2,

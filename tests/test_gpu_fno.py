@@ -133,7 +133,7 @@ def test_forward_and_backward_match_oracle(torch):
     ref, cache = fo.forward(p, x, prior, m, bf16=True)
     got = unpacked(out[:, None], N)
     assert rel(got, ref) < 5e-4
-    loss, errs = model.loss(out, tt, B)
+    loss, errs = model.loss(out, tt, B, grad_scale=1.0)
     ref_loss, ref_e, gout = fo.relative_loss(ref, target)
     assert abs(float(loss.item()) - ref_loss) <= 1e-4 * ref_loss
     model.grad.zero_()
@@ -161,17 +161,35 @@ def test_adam_matches_formula(torch):
     assert np.allclose(ts[0].cpu().numpy(), ref, rtol=1e-5, atol=1e-7)
 
 
-def test_training_beats_the_coarse_prior(torch):
-    """A small surrogate trained for a few hundred steps on pairs from the plain split step
-    predicts held-out jumps better than the coarse split step it corrects."""
-    from wavefunctionsimpython_gb300.fno import FNO, FnoConfig, evaluate, make_dataset, train
+def test_training_learns_free_propagation(torch):
+    """With the identity as prior, a small network trained on free-particle pairs from the
+    split step learns the 20-step propagator: held-out error drops from ~2 % to well below 1 %."""
+    from wavefunctionsimpython_gb300.fno import FNO, FnoConfig, ScenarioRanges, evaluate, make_dataset, train
 
-    cfg = FnoConfig(N=32, extent=40.0, width=8, modes=6, layers=2, hidden=16, jump_steps=20, prior_steps=1)
-    data = make_dataset(cfg, npairs=192, windows=4, group=16, seed=11)
-    held = make_dataset(cfg, npairs=32, windows=2, group=16, seed=12345, gen=data[3])
-    model = FNO(cfg, seed=3)
-    info = train(model, data[:3], batch=8, steps=300, lr=3e-3, warmup=20)
-    assert info["steps"] == 300
+    cfg = FnoConfig(N=32, width=8, modes=6, layers=2, hidden=16, jump_steps=20, prior_steps=0)
+    rg = ScenarioRanges(p_wall=0.0, p_ho=0.0, sigma=(2.0, 3.0), x0=(-4.0, 4.0), k0=(0.0, 0.3))
+    data = make_dataset(cfg, npairs=768, windows=6, group=64, seed=1, ranges=rg)
+    held = make_dataset(cfg, npairs=128, windows=2, group=64, seed=999, gen=data[3], ranges=rg)
+    model = FNO(cfg, seed=0)
+    info = train(model, data[:3], batch=8, steps=1000, lr=1e-3, warmup=100)
+    assert info["steps"] == 1000
     ev = evaluate(model, held[:3], batch=16)
     assert np.all(np.isfinite(ev["err_net"]))
-    assert ev["err_net"].mean() < 0.8 * ev["err_prior"].mean(), (ev["err_net"].mean(), ev["err_prior"].mean())
+    assert ev["err_prior"].mean() > 0.01
+    assert ev["err_net"].mean() < 0.25 * ev["err_prior"].mean(), (ev["err_net"].mean(), ev["err_prior"].mean())
+
+
+def test_training_beats_the_coarse_prior(torch):
+    """Harmonic oscillators whose packets stay inside the kept modes: the trained network
+    corrects the one-step coarse split step of a 50-step jump on held-out seeds."""
+    from wavefunctionsimpython_gb300.fno import FNO, FnoConfig, ScenarioRanges, evaluate, make_dataset, train
+
+    cfg = FnoConfig(N=32, extent=24.0, width=8, modes=8, layers=2, hidden=16, jump_steps=50, prior_steps=1)
+    rg = ScenarioRanges(p_wall=0.0, p_ho=1.0, omega=(0.2, 0.5), sigma=(1.5, 2.5), x0=(-2.0, -1.0), k0=(0.2, 0.6))
+    data = make_dataset(cfg, npairs=768, windows=6, group=64, seed=11, ranges=rg)
+    held = make_dataset(cfg, npairs=128, windows=2, group=64, seed=12345, gen=data[3], ranges=rg)
+    model = FNO(cfg, seed=3)
+    train(model, data[:3], batch=8, steps=1500, lr=1e-3, warmup=100)
+    ev = evaluate(model, held[:3], batch=16)
+    assert np.all(np.isfinite(ev["err_net"]))
+    assert ev["err_net"].mean() < 0.7 * ev["err_prior"].mean(), (ev["err_net"].mean(), ev["err_prior"].mean())

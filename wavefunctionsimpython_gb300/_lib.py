@@ -156,7 +156,7 @@ def load(path: str | os.PathLike | None = None):
         "wfs_fno_spectral_weight_grad": ([vp, vp, vp, i32, i32, i32, vp], C.c_int),
         "wfs_fno_adam": ([vp, vp, vp, vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp],
                          C.c_int),
-        "wfs_fno_loss": ([vp, vp, i64, i32, vp, vp, vp, vp], C.c_int),
+        "wfs_fno_loss": ([vp, vp, i64, i32, C.c_float, vp, vp, vp, vp], C.c_int),
         "wfs_fno_sample_norms": ([vp, vp, i64, i32, vp, vp, vp], C.c_int),
         "wfs_fno_make_input": ([vp, vp, C.c_float, vp, vp, i32, i64, vp], C.c_int),
         "wfs_fno_scale_samples": ([vp, vp, i32, i32, i64, vp], C.c_int),

@@ -252,19 +252,27 @@ __global__ void gather_kernel(const float2* __restrict__ spec, float2* __restric
 
 // Pull form over the kept modes and their mirrors (no write conflicts):
 // Y(k) = (Za(k) + conj Za(-k)) / 2 + i (Zb(k) + conj Zb(-k)) / 2, Z = 0 off the kept set.
+// The kept x (and y) set [0, m) u [N-m, N) is not closed under negation (the mirror of
+// N-m is m), so the written x and y indices are [0, m] u [N-m, N) when 2m < N (2m + 1
+// values; all N when 2m = N) and the z indices [0, m) u (N-m, N).
+__host__ __device__ __forceinline__ int mirror_span(int N, int m) { return 2 * m < N ? 2 * m + 1 : 2 * m; }
+__device__ __forceinline__ int mirror_index(int i, int N, int m) {
+    return (2 * m < N && i > m) ? N - 2 * m - 1 + i : i;
+}
 __global__ void scatter_kernel(const float2* __restrict__ Zm, float2* __restrict__ spec, int B, int C, int N, int m) {
     const int P = C / 2;
     const int nz = 2 * m - 1;
-    const int64_t npos = int64_t(2 * m) * (2 * m) * nz;
+    const int nxy = mirror_span(N, m);
+    const int64_t npos = int64_t(nxy) * nxy * nz;
     const int64_t n3 = int64_t(N) * N * N;
     const int64_t total = npos * B * P;
     for (int64_t g = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; g < total; g += int64_t(gridDim.x) * blockDim.x) {
         const int j = int(g % P);
         const int b = int((g / P) % B);
         const int64_t ip = g / (int64_t(P) * B);
-        const int iz = int(ip % nz), iy = int((ip / nz) % (2 * m)), ix = int(ip / (int64_t(nz) * 2 * m));
-        const int kx = ix < m ? ix : N - 2 * m + ix;
-        const int ky = iy < m ? iy : N - 2 * m + iy;
+        const int iz = int(ip % nz), iy = int((ip / nz) % nxy), ix = int(ip / (int64_t(nz) * nxy));
+        const int kx = mirror_index(ix, N, m);
+        const int ky = mirror_index(iy, N, m);
         const int kz = iz < m ? iz : N - m + 1 + (iz - m);
         const int mp = mode_of(kx, ky, kz, N, m);
         const int mn = mode_of((N - kx) % N, (N - ky) % N, (N - kz) % N, N, m);
@@ -436,8 +444,9 @@ __global__ void __launch_bounds__(256) loss_partial_kernel(const float* __restri
         part[2 * blockIdx.x + 1] = c;
     }
 }
-__global__ void loss_finish_kernel(const double* __restrict__ part, int B, float* __restrict__ sample_err,
-                                   float* __restrict__ loss, float* __restrict__ scale_out) {
+__global__ void loss_finish_kernel(const double* __restrict__ part, int B, float grad_scale,
+                                   float* __restrict__ sample_err, float* __restrict__ loss,
+                                   float* __restrict__ scale_out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double total = 0.0;
     for (int b = 0; b < B; ++b) {
@@ -448,7 +457,7 @@ __global__ void loss_finish_kernel(const double* __restrict__ part, int B, float
         }
         if (c <= 0.0) c = 1.0;
         sample_err[b] = float(a / c);
-        scale_out[b] = float(2.0 / (double(B) * c));
+        scale_out[b] = float(double(grad_scale) * 2.0 / (double(B) * c));
         total += a / c;
     }
     *loss = float(total / B);
@@ -702,7 +711,8 @@ int wfs_fno_scatter(const void* Zm, void* spec, int32_t B, int32_t C, int32_t N,
     cudaStream_t s = (cudaStream_t)stream;
     const int64_t n3 = int64_t(N) * N * N;
     if (cudaMemsetAsync(spec, 0, size_t(B) * (C / 2) * n3 * sizeof(float2), s) != cudaSuccess) return WFS_ERR_CUDA;
-    const int64_t total = int64_t(2 * m) * (2 * m) * (2 * m - 1) * B * (C / 2);
+    const int nxy = mirror_span(N, m);
+    const int64_t total = int64_t(nxy) * nxy * (2 * m - 1) * B * (C / 2);
     scatter_kernel<<<grid_for(total), 256, 0, s>>>((const float2*)Zm, (float2*)spec, B, C, N, m);
     return status_of(cudaGetLastError());
 }
@@ -753,9 +763,10 @@ int wfs_fno_adam(float* p, const float* g, float* m1, float* m2, int64_t n, floa
     return status_of(cudaGetLastError());
 }
 
-int wfs_fno_loss(const float* pred, const float* target, int64_t per_sample, int32_t B, float* sample_err, float* grad,
-                 float* loss, void* stream) {
-    if (!pred || !target || !sample_err || !loss || per_sample < 1 || B < 1) return WFS_ERR_ARG;
+int wfs_fno_loss(const float* pred, const float* target, int64_t per_sample, int32_t B, float grad_scale,
+                 float* sample_err, float* grad, float* loss, void* stream) {
+    if (!pred || !target || !sample_err || !loss || per_sample < 1 || B < 1 || !(grad_scale > 0.f))
+        return WFS_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t part_bytes = ((size_t(B) * kLossSlices * 2 * sizeof(double) + 255) / 256) * 256;
     char* scr = (char*)scratch_for(part_bytes + size_t(B) * sizeof(float));
@@ -763,7 +774,7 @@ int wfs_fno_loss(const float* pred, const float* target, int64_t per_sample, int
     double* part = (double*)scr;
     float* scale = (float*)(scr + part_bytes);
     loss_partial_kernel<<<B * kLossSlices, 256, 0, s>>>(pred, target, per_sample, part);
-    loss_finish_kernel<<<1, 32, 0, s>>>(part, B, sample_err, loss, scale);
+    loss_finish_kernel<<<1, 32, 0, s>>>(part, B, grad_scale, sample_err, loss, scale);
     if (grad) loss_grad_kernel<<<grid_for(int64_t(B) * per_sample), 256, 0, s>>>(pred, target, per_sample, B, scale, grad);
     return status_of(cudaGetLastError());
 }

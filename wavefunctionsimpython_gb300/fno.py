@@ -263,11 +263,14 @@ class FNO:
                                           n3, s), "lift backward")
         self._wgrad(ga, c, x, 4, "W0", B)
 
-    def loss(self, pred, target, B, grad=True):
+    def loss(self, pred, target, B, grad=True, grad_scale=None):
         """Mean relative squared error over the batch (device scalar) and, when grad,
-        d loss / d pred in the workspace's gout."""
+        grad_scale * d loss / d pred in the workspace's gout. The default scale (elements
+        per sample) makes it the gradient of the per-element relative error."""
         ws = self.ws
-        self._ck(self.lib.wfs_fno_loss(_ptr(pred), _ptr(target), 2 * self.cfg.n3, B, _ptr(ws["sample_err"]),
+        per = 2 * self.cfg.n3
+        gs = float(per if grad_scale is None else grad_scale)
+        self._ck(self.lib.wfs_fno_loss(_ptr(pred), _ptr(target), per, B, gs, _ptr(ws["sample_err"]),
                                        _ptr(ws["gout"]) if grad else None, _ptr(ws["loss"]), self._s()), "loss")
         return ws["loss"], ws["sample_err"][:B]
 
@@ -299,24 +302,41 @@ def harmonic_potential(N, extent, omega, mass=1.0):
 
 @dataclass
 class Scenario:
-    kind: str          # "wall" or "ho"
+    kind: str          # "wall", "ho" or "free"
     strength: float    # barrier height (Hartree) or omega
-    width: float       # barrier thickness (Bohr); 0 for "ho"
+    width: float       # barrier thickness (Bohr); 0 otherwise
     sigma: float
     x0: float
     k0: float
 
 
-def draw_scenarios(n, rng):
-    """Barriers with the batched sweep's ranges (height U[0.2,2] Ha, thickness U[1,4] Bohr) and
-    harmonic oscillators with omega U[0.2,0.8]; packets sigma U[1,3], x0 U[-12,-6], k0x U[0.5,3]."""
+@dataclass
+class ScenarioRanges:
+    """Uniform ranges the scenarios are drawn from. The defaults are the barrier ranges of
+    the batched sweep (height U[0.2,2] Ha, thickness U[1,4] Bohr) and harmonic oscillators
+    with omega U[0.2,0.8], packets sigma U[1,3], x0 U[-12,-6], k0x U[0.5,3], half of each."""
+    p_wall: float = 0.5
+    p_ho: float = 0.5
+    height: tuple = (0.2, 2.0)
+    thickness: tuple = (1.0, 4.0)
+    omega: tuple = (0.2, 0.8)
+    sigma: tuple = (1.0, 3.0)
+    x0: tuple = (-12.0, -6.0)
+    k0: tuple = (0.5, 3.0)
+
+
+def draw_scenarios(n, rng, ranges: ScenarioRanges | None = None):
+    r = ranges or ScenarioRanges()
     out = []
     for _ in range(n):
-        if rng.uniform() < 0.5:
-            kind, st, w = "wall", rng.uniform(0.2, 2.0), rng.uniform(1.0, 4.0)
+        u = rng.uniform()
+        if u < r.p_wall:
+            kind, st, w = "wall", rng.uniform(*r.height), rng.uniform(*r.thickness)
+        elif u < r.p_wall + r.p_ho:
+            kind, st, w = "ho", rng.uniform(*r.omega), 0.0
         else:
-            kind, st, w = "ho", rng.uniform(0.2, 0.8), 0.0
-        out.append(Scenario(kind, st, w, rng.uniform(1.0, 3.0), rng.uniform(-12.0, -6.0), rng.uniform(0.5, 3.0)))
+            kind, st, w = "free", 0.0, 0.0
+        out.append(Scenario(kind, st, w, rng.uniform(*r.sigma), rng.uniform(*r.x0), rng.uniform(*r.k0)))
     return out
 
 
@@ -350,6 +370,8 @@ class PairGenerator:
         cfg = self.cfg
         if sc.kind == "ho":
             return harmonic_potential(cfg.N, cfg.extent, sc.strength, cfg.mass)
+        if sc.kind == "free":
+            return np.zeros((cfg.N,) * 3, np.complex64)
         self.builder.potential_clear()
         self.builder.add_wall(sc.strength, (0.0, 0.0, 0.0), (1.0, 0.0, 0.0), sc.width)
         return self.builder.get_potential()
@@ -370,7 +392,11 @@ class PairGenerator:
             self.exact.get_psi_device(i, out[i].data_ptr())
 
     def coarse_jump(self, psi_in, out):
+        """prior_steps coarse Strang steps over the jump; prior_steps = 0 is the identity."""
         cfg = self.cfg
+        if cfg.prior_steps == 0:
+            out.copy_(psi_in)
+            return
         for i in range(self.G):
             self.coarse.set_psi_device(i, psi_in[i].data_ptr())
         T = cfg.jump_steps * cfg.dt
@@ -407,8 +433,10 @@ class PairGenerator:
             self.normalise(self.psi, x_out[rows], prior_out[rows], target_out[rows])
 
 
-def make_dataset(cfg: FnoConfig, npairs, windows, group, seed, device="cuda", stream=None, gen=None):
-    """npairs (a multiple of windows * group) normalised training triples on the device."""
+def make_dataset(cfg: FnoConfig, npairs, windows, group, seed, device="cuda", stream=None, gen=None,
+                 ranges: ScenarioRanges | None = None):
+    """npairs (a multiple of windows * group) normalised training triples on the device,
+    plus the generator and the scenario of every pair (row start + w * G + i)."""
     import torch
 
     rng = np.random.default_rng(seed)
@@ -419,16 +447,23 @@ def make_dataset(cfg: FnoConfig, npairs, windows, group, seed, device="cuda", st
     x = torch.empty((npairs, 2, cfg.n3), **c64)
     prior = torch.empty((npairs, cfg.n3), **c64)
     target = torch.empty((npairs, cfg.n3), **c64)
+    scen = []
     for k in range(npairs // per):
-        gen.trajectories(draw_scenarios(group, rng), windows, x, prior, target, start=k * per)
-    return x, prior, target, gen
+        sc = draw_scenarios(group, rng, ranges)
+        gen.trajectories(sc, windows, x, prior, target, start=k * per)
+        scen += sc * windows
+    return x, prior, target, gen, scen
 
 
-def train(model: FNO, data, batch, steps, lr, warmup=50, log_every=0, time_budget=None, seed=0):
-    """Adam over random mini-batches of the dataset with a cosine learning-rate decay."""
+def train(model: FNO, data, batch, steps, lr, warmup=50, log_every=0, time_budget=None, seed=0, step_offset=0,
+          total_steps=None):
+    """Adam over random mini-batches of the dataset with a linear warm-up and a cosine
+    learning-rate decay over total_steps (default steps); step_offset continues one
+    schedule across several datasets."""
     torch = model.torch
     x, prior, target = data
     n = x.shape[0]
+    total = total_steps or steps
     g = torch.Generator(device="cpu").manual_seed(seed)
     bx = torch.empty((batch, 2, model.cfg.n3), dtype=torch.complex64, device=x.device)
     bp = torch.empty((batch, model.cfg.n3), dtype=torch.complex64, device=x.device)
@@ -441,11 +476,12 @@ def train(model: FNO, data, batch, steps, lr, warmup=50, log_every=0, time_budge
         torch.index_select(x, 0, idx, out=bx)
         torch.index_select(prior, 0, idx, out=bp)
         torch.index_select(target, 0, idx, out=bt)
-        f = min(1.0, (it + 1) / max(1, warmup)) * 0.5 * (1.0 + math.cos(math.pi * it / max(1, steps)))
+        gi = step_offset + it
+        f = min(1.0, (gi + 1) / max(1, warmup)) * 0.5 * (1.0 + math.cos(math.pi * min(gi, total) / max(1, total)))
         loss = model.train_step(bx, bp, bt, batch, lr * f)
         done += 1
         if log_every and (it % log_every == 0 or it == steps - 1):
-            history.append((it, float(loss.item())))
+            history.append((gi, float(loss.item())))
         if time_budget is not None and time.perf_counter() - t0 > time_budget:
             break
     model.stream.synchronize()
