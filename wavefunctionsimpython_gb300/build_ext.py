@@ -40,7 +40,8 @@ def _sources():
 
 
 def _deps_mtime():
-    files = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [ROOT / "include" / "wfs.h", Path(__file__)]
+    files = (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h"))
+             + list((ROOT / "include").glob("*.h")) + [Path(__file__)])
     return max(f.stat().st_mtime for f in files)
 
 

@@ -17,6 +17,8 @@
 // gives each CTA W whole rows.
 #pragma once
 
+#include <cstdlib>
+
 #include "kernels.h"
 
 namespace wfs {
@@ -212,6 +214,99 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_strided_ker
 }
 
 // ---------------------------------------------------------------------------
+// Pipelined strided pass: persistent CTAs walk the (outer, tile) items with a
+// stride of gridDim.x; while a CTA transforms item k from shared memory, the
+// cp.async copies of item k + gridDim.x are in flight, so HBM reads overlap the
+// register FFTs instead of alternating with them. Each thread stages exactly
+// the elements it later reads (rows t + P*i of its column), so the staging
+// buffers need no block barrier: cp.async.wait_group orders a thread's own
+// copies before its reads.
+// Shared memory: the transpose buffer plus two staging tiles (3 L W elements).
+// ---------------------------------------------------------------------------
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    if constexpr (BYTES == 16) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+    } else {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES) : "memory");
+    }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename R, int P, int Q, int W, int OP>
+__global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS)
+    fft_strided_pipe_kernel(const PassArgs<R> a, int64_t nitems) {
+    constexpr int L = P * Q;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Cx<R>* sm = reinterpret_cast<Cx<R>*>(smem_raw);
+    Cx<R>* stage = sm + L * W;  // [2][L][W]
+    const int tid = threadIdx.x, c = tid % W, t = tid / W;
+    const int rs = int(a.row_stride);
+    auto issue = [&](int64_t item, int slot) {
+        const int tile = int(item % a.tiles);
+        const int64_t outer = item / a.tiles;
+        const int col = tile * W + c;
+        if (t < P && col < a.ncols) {
+            const Cx<R>* src = a.data + outer * a.outer_stride + col;
+            Cx<R>* dst = stage + slot * (L * W) + c;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) cp_async_elem<sizeof(Cx<R>)>(dst + (t + P * i) * W, src + (t + P * i) * rs);
+        }
+        cp_async_commit();
+    };
+    auto sidx_f = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
+    auto sidx_i = [&](int k2, int n1) { return (k2 * Q + n1) * W + c; };
+    int64_t item = blockIdx.x;
+    if (item < nitems) issue(item, 0);
+    int slot = 0;
+    for (; item < nitems; item += gridDim.x) {
+        const int64_t next = item + gridDim.x;
+        if (next < nitems) issue(next, slot ^ 1);
+        else cp_async_commit();
+        cp_async_wait<1>();
+        const int tile = int(item % a.tiles);
+        const int64_t outer = item / a.tiles;
+        const int col = tile * W + c;
+        const bool active = col < a.ncols;
+        Cx<R>* base = a.data + outer * a.outer_stride + col;
+        const Cx<R>* src = stage + slot * (L * W) + c;
+        Cx<R> a1[Q], a2[P];
+        if (t < P) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) a1[i] = active ? src[(t + P * i) * W] : mk<R>(R(0), R(0));
+        }
+        if constexpr (OP == OP_PLAIN) {
+            if (a.dir < 0) two_stage<P, Q, -1, R>(a1, a2, sm, a.tw, t, sidx_f);
+            else two_stage<P, Q, +1, R>(a1, a2, sm, a.tw, t, sidx_f);
+            if (active && t < Q) {
+#pragma unroll
+                for (int k = 0; k < P; ++k) base[(t + Q * k) * rs] = scale(a2[k], a.scale);
+            }
+        } else {  // OP_KIN
+            two_stage<P, Q, -1, R>(a1, a2, sm, a.tw, t, sidx_f);
+            if (t < Q) {
+                Cx<R> cf = mk<R>(R(0), R(0));
+                if (active) cf = scale(cmul(a.k_c1[col / a.c2n], a.k_c2[col % a.c2n]), a.scale);
+#pragma unroll
+                for (int k = 0; k < P; ++k) a2[k] = cmul(a2[k], cmul(a.k_row[t + Q * k], cf));
+            }
+            __syncthreads();
+            two_stage<Q, P, +1, R>(a2, a1, sm, a.tw, t, sidx_i);
+            if (active && t < P) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) base[(t + P * i) * rs] = a1[i];
+            }
+        }
+        __syncthreads();  // the next item's stage 1 rewrites the transpose buffer
+        slot ^= 1;
+    }
+    cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
 // Contiguous pass (z axis)
 // ---------------------------------------------------------------------------
 template <typename R, int P, int Q, int W, int OP>
@@ -313,12 +408,58 @@ struct ContigW {
     static constexpr int value = (256 / T) > 0 ? (256 / T) : 1;
 };
 
+// The pipelined strided pass is used where its three L x W tiles leave room for two
+// CTAs per SM; WFS_STRIDED_PIPELINE=0 in the environment selects the plain kernel
+// (for A/B timing).
+inline bool strided_pipeline_enabled() {
+    static const int on = [] {
+        const char* e = getenv("WFS_STRIDED_PIPELINE");
+        return (e && e[0] == '0') ? 0 : 1;
+    }();
+    return on != 0;
+}
+inline int device_sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+            n = v;
+    }
+    return n > 0 ? n : 1;
+}
+
+template <typename R, int L, int OP>
+cudaError_t run_strided_pipe(const PassArgs<R>& a, int64_t outer_count, cudaStream_t s) {
+    constexpr int P = PlanOf<L>::P, Q = PlanOf<L>::Q, T = cmax(P, Q);
+    constexpr int W = StridedW<R, T>::value;
+    const size_t smem = 3 * size_t(L) * W * sizeof(Cx<R>);
+    auto kern = fft_strided_pipe_kernel<R, P, Q, W, OP>;
+    static int blocks_per_sm = 0;
+    if (blocks_per_sm == 0) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        int nb = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, T * W, smem);
+        if (e != cudaSuccess) return e;
+        blocks_per_sm = nb > 0 ? nb : 1;
+    }
+    const int64_t nitems = outer_count * a.tiles;
+    const int64_t cap = int64_t(blocks_per_sm) * device_sm_count();
+    const int64_t grid = nitems < cap ? nitems : cap;
+    kern<<<dim3(unsigned(grid)), dim3(T * W), smem, s>>>(a, nitems);
+    return cudaGetLastError();
+}
+
 template <typename R, int L, int OP>
 cudaError_t run_strided(const PassArgs<R>& a0, int64_t outer_count, cudaStream_t s) {
     constexpr int P = PlanOf<L>::P, Q = PlanOf<L>::Q, T = cmax(P, Q);
     constexpr int W = StridedW<R, T>::value;
     PassArgs<R> a = a0;
     a.tiles = (a.ncols + W - 1) / W;
+    if constexpr (3 * size_t(L) * W * sizeof(Cx<R>) <= 112 * 1024) {
+        if (strided_pipeline_enabled() && outer_count * a.tiles > int64_t(2) * device_sm_count())
+            return run_strided_pipe<R, L, OP>(a, outer_count, s);
+    }
     const size_t smem = size_t(L) * W * sizeof(Cx<R>);
     auto kern = fft_strided_kernel<R, P, Q, W, OP>;
     static bool attr_set = false;
