@@ -125,3 +125,51 @@ def test_power_series_method_through_sim_state(tmp_path):
         s.evolve_state()
     ref = orc.taylor_step(psi, V, dx, 0.002, 1.0, order=10, stencil_order=2, nsteps=3)
     assert np.linalg.norm(s.get_wave_function() - ref) / np.linalg.norm(ref) < 1e-5
+
+
+@pytest.mark.parametrize("method", ["fourier", "power_series"])
+def test_checkpoint_resume_is_exact_with_moving_wall(tmp_path, method):
+    """A run checkpointed after 5 steps and resumed in a fresh SimState ends bit-identical
+    to the uninterrupted run, moving wall and iteration counters included."""
+    from wavefunctionsimpython_gb300 import iter_data as idm
+    from wavefunctionsimpython_gb300 import sim_state as ssm
+
+    cfg = base_config(tmp_path, method=method, dbl=False)
+    cfg["simulation"]["is_dynamic_potential_mode"] = True
+    cfg["potential"]["walls"][0]["velocity_bohr_radius_hartree_per_h_bar_3"] = [0.5, 0.0, 0.0]
+
+    def advance(s, it, n):
+        for _ in range(n):
+            s.evolve_state()
+            s.update_potential()
+            it.i += 1
+            it.total_simulated_time += s.get_delta_time_h_bar_per_hartree()
+
+    a = ssm.SimState(copy.deepcopy(cfg))
+    a.set_use_cache(False)
+    a.initialize_state()
+    ita = idm.IterData(cfg)
+    advance(a, ita, 5)
+    ckpt = str(tmp_path / "state.npz")
+    a.save_checkpoint(ckpt, ita)
+    advance(a, ita, 4)
+    ref_psi, ref_v = a.get_wave_function(), a.engine.get_potential()
+
+    b = ssm.SimState(copy.deepcopy(cfg))
+    b.set_use_cache(False)
+    b.initialize_state()
+    itb = idm.IterData(cfg)
+    b.load_checkpoint(ckpt, itb)
+    assert itb.i == 5
+    advance(b, itb, 4)
+    assert itb.i == ita.i and itb.total_simulated_time == ita.total_simulated_time
+    assert np.array_equal(b.engine.get_potential(), ref_v)
+    assert np.array_equal(b.get_wave_function(), ref_psi)
+    assert np.allclose(b.get_potential_walls()[0].center_bohr_radii_3, a.get_potential_walls()[0].center_bohr_radii_3)
+
+    other = copy.deepcopy(cfg)
+    other["volume"]["number_of_voxels_3"] = [32, 32, 32]
+    c = ssm.SimState(other)
+    c.set_use_cache(False)
+    with pytest.raises(ValueError):
+        c.load_checkpoint(ckpt)

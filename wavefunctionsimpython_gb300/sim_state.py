@@ -298,6 +298,52 @@ class SimState:
             self.engine.step_taylor(nsteps, self.__delta_time_h_bar_per_hartree, self.get_particle_mass(),
                                     self.__order_of_approximation, self.__stencil_order)
 
+    # ---------------------------------------------------------- checkpoint
+    CHECKPOINT_VERSION = 1
+
+    def save_checkpoint(self, path, iter_data=None):
+        """Writes psi, V, the moving walls and the iteration counters to one .npz file so
+        a run resumes exactly where it stopped. The reference has no working psi
+        checkpoint (its snapshot writer is commented out, sources/snapshot_io.py:12-16)."""
+        eng = self.engine
+        walls = np.array([np.concatenate([w.center_bohr_radii_3, w.velocity_bohr_radius_hartree_per_h_bar_3,
+                                          [float(w.potential_hartree)]]) for w in self.__potential_walls],
+                         dtype=np.float64).reshape(-1, 7)
+        it = {} if iter_data is None else {"i": iter_data.i, "total_simulated_time": iter_data.total_simulated_time,
+                                          "elapsed_system_time_s": iter_data.elapsed_system_time_s}
+        np.savez(path, version=self.CHECKPOINT_VERSION, psi=eng.get_psi(), potential=eng.get_potential(),
+                 number_of_voxels_3=np.asarray(self.__number_of_voxels_3, dtype=np.int64),
+                 volume_bohr_radii_3=np.asarray(self.__simulated_volume_dimensions_bohr_radii_3, dtype=np.float64),
+                 double_precision=self.__double_precision, delta_time=self.__delta_time_h_bar_per_hartree,
+                 walls=walls, iteration=np.asarray([it.get("i", 0)], dtype=np.int64),
+                 times=np.asarray([it.get("total_simulated_time", 0.0), it.get("elapsed_system_time_s", 0.0)]))
+
+    def load_checkpoint(self, path, iter_data=None):
+        """Restores a file written by save_checkpoint: psi and V on the GPU, the walls'
+        positions, and (when given) the IterData counters. Raises ValueError when the
+        checkpoint's grid, extent, precision or wall count differ from this state's."""
+        with np.load(path) as f:
+            if int(f["version"]) != self.CHECKPOINT_VERSION:
+                raise ValueError(f"unsupported checkpoint version {int(f['version'])}")
+            if (tuple(int(x) for x in f["number_of_voxels_3"]) != tuple(int(x) for x in self.__number_of_voxels_3)
+                    or not np.allclose(f["volume_bohr_radii_3"], self.__simulated_volume_dimensions_bohr_radii_3)
+                    or bool(f["double_precision"]) != bool(self.__double_precision)):
+                raise ValueError("checkpoint grid, extent or precision differ from this simulation")
+            walls = f["walls"]
+            if walls.shape[0] != len(self.__potential_walls):
+                raise ValueError("checkpoint wall count differs from this simulation")
+            eng = self._make_engine()
+            eng.set_psi(f["psi"])
+            eng.set_potential(f["potential"])
+            for w, row in zip(self.__potential_walls, walls):
+                w.center_bohr_radii_3 = row[0:3].copy()
+                w.velocity_bohr_radius_hartree_per_h_bar_3 = row[3:6].copy()
+                w.potential_hartree = float(row[6])
+            if iter_data is not None:
+                iter_data.i = int(f["iteration"][0])
+                iter_data.total_simulated_time = float(f["times"][0])
+                iter_data.elapsed_system_time_s = float(f["times"][1])
+
     def get_simulation_method_text(self, use_colors=False):
         text = io.StringIO()
         if self.__simulation_method == SimulationMethod.FOURIER:
