@@ -592,6 +592,35 @@ def run_surrogate(args):
     return 0
 
 
+def run_render(args):
+    """Headless volume view of the double slit after 200 steps: 1024 x 768 frames of psi and V
+    (the reference's canvas size and step 0.1), without shadows and with the 50-step shadow march."""
+    import torch
+    from wavefunctionsimpython_gb300._lib import render_desc
+
+    torch.cuda.set_device(args.device)
+    stream = engine_stream(torch)
+    e = build_engine(args.device, stream.cuda_stream)
+    e.step_split(200, DT, 1.0)
+    e.synchronize()
+    out = {}
+    for name, (w, h, shadows, reps) in {"frame_1024x768": (1024, 768, 0, 5),
+                                         "frame_1024x768_shadows50": (1024, 768, 50, 1)}.items():
+        d = render_desc(w, h, azimuth=30.0, shadow_steps=shadows)
+        e.render(d)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            img = e.render(d)
+        out[name] = {"ms_per_frame": 1e3 * (time.perf_counter() - t0) / reps,
+                     "mean_rgb": [float(v) for v in img[:, :, :3].reshape(-1, 3).mean(axis=0)]}
+    line = {"metric": "headless volume render ms/frame (256^3 double slit, 1024x768, step 0.1 voxel)",
+            "value": out["frame_1024x768"]["ms_per_frame"], "unit": "ms", "n_gpus": 1, "higher_is_better": False,
+            "dtype": "f32", "data": "synthetic", "config": {"workload": "ray march of psi and V, host round trip included"},
+            "frames": out}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -602,9 +631,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", choices=["auto", "axis", "plane"], default="auto",
                     help="split-step schedule: fused yz-plane pass (auto) or one pass per axis")
-    ap.add_argument("--workload", choices=["split", "taylor", "batch", "surrogate"], default="split",
+    ap.add_argument("--workload", choices=["split", "taylor", "batch", "surrogate", "render"], default="split",
                     help="split: the headline 256^3 double slit; taylor: the 128^3 power-series workload; "
-                         "batch: the 256-instance uneven sweep; surrogate: train and measure the FNO jump")
+                         "batch: the 256-instance uneven sweep; surrogate: train and measure the FNO jump; "
+                         "render: headless volume view frames")
     ap.add_argument("--fno-dist", choices=["inband", "sweep"], default="inband",
                     help="surrogate scenarios: oscillators inside the kept modes, or the sweep's barriers and "
                          "oscillators on a 40-Bohr box")
@@ -623,6 +653,8 @@ def main():
         return run_batch(args)
     if args.workload == "surrogate":
         return run_surrogate(args)
+    if args.workload == "render":
+        return run_render(args)
     return run_own(args)
 
 

@@ -238,6 +238,36 @@ int wfs_batch_launch_count(wfs_batch* b, int64_t* out);
 int wfs_observe_noalloc(const void* psi_device, int32_t dtype, const int32_t n[3], const double extent[3],
                         const wfs_box* boxes, int32_t nbox, const wfs_box* loc, double* out_device, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Headless volume rendering of psi and V (replaces the vispy/GLSL view of
+ * sources/volumetric_visualization.py:38-200 and
+ * sources/multi_volume_shaders.py:200-390 with a CUDA ray march into an image
+ * buffer; no graphics API). Row-major image, height x width pixels.
+ * ---------------------------------------------------------------------- */
+typedef struct wfs_render_desc {
+    int32_t width, height;        /* image size (the reference's canvas: 1024 x 768) */
+    double azimuth_deg;           /* turntable camera around the +y axis (array axis 1) */
+    double elevation_deg;         /* the reference's default: 45 */
+    double fov_deg;               /* the reference's default: 45 */
+    double distance;              /* camera distance in voxels; <= 0 fits the volume */
+    double relative_step;         /* ray step in voxels (the reference: 0.1) */
+    double wave_function_scale;   /* |Re psi|, |Im psi| mapped to [-1, 1]; <= 0 means 0.005 */
+    double potential_scale;       /* <= 0: max |V| over its real and imaginary parts */
+    double light[3];              /* direction towards the light (the reference: 1, 1, -1) */
+    int32_t shadow_steps;         /* 0: no shadows; the reference marches 50 (0..1000) */
+    int32_t show_potential;       /* 1: render V's volume too */
+    int32_t format;               /* 0: RGBA8 (4 bytes per pixel), 1: RGBA float32 */
+} wfs_render_desc;
+
+/* Renders the handle's psi (materialised first) and V into `image`
+ * (width * height * 4 bytes for RGBA8, 16 for float; host or device memory). */
+int wfs_render(wfs_handle* h, const wfs_render_desc* desc, void* image, int32_t to_device);
+
+/* The same for caller-owned device arrays: psi (complex64/complex128, [n0][n1][n2])
+ * and V (complex64, may be NULL); asynchronous on `stream`. */
+int wfs_render_volume(const void* psi_device, int32_t dtype, const int32_t n[3], const void* potential_device,
+                      const wfs_render_desc* desc, void* image_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

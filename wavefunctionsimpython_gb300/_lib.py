@@ -38,6 +38,7 @@ EXPORTED = [
     "wfs_batch_init_gaussian", "wfs_batch_add_wall", "wfs_batch_add_absorbing", "wfs_batch_set_potential",
     "wfs_batch_set_psi", "wfs_batch_get_psi", "wfs_batch_run", "wfs_batch_observe", "wfs_batch_set_config",
     "wfs_batch_autotune", "wfs_batch_launch_count", "wfs_observe_noalloc", "wfs_plane_current",
+    "wfs_render", "wfs_render_volume",
 ]
 # Every entry point include/wfs_fno.h declares (the surrogate's kernels).
 FNO_EXPORTED = [
@@ -85,6 +86,27 @@ class BatchDesc(C.Structure):
 
 
 _lib = None
+
+
+class RenderDesc(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("azimuth_deg", C.c_double),
+                ("elevation_deg", C.c_double), ("fov_deg", C.c_double), ("distance", C.c_double),
+                ("relative_step", C.c_double), ("wave_function_scale", C.c_double),
+                ("potential_scale", C.c_double), ("light", C.c_double * 3), ("shadow_steps", C.c_int32),
+                ("show_potential", C.c_int32), ("format", C.c_int32)]
+
+
+def render_desc(width=1024, height=768, azimuth=0.0, elevation=45.0, fov=45.0, distance=0.0, relative_step=0.1,
+                wave_function_scale=0.005, potential_scale=0.0, light=(1.0, 1.0, -1.0), shadow_steps=0,
+                show_potential=True, float_output=False) -> RenderDesc:
+    """Render settings with the reference's defaults (sources/volumetric_visualization.py,
+    sources/multi_volume_visual.py): 1024 x 768, elevation 45, fov 45, step 0.1 voxel,
+    colour limit 0.005, light (1, 1, -1). Shadows (the reference's 50-step march per
+    sample) are off by default because they multiply the cost by ~100."""
+    return RenderDesc(int(width), int(height), float(azimuth), float(elevation), float(fov), float(distance),
+                      float(relative_step), float(wave_function_scale), float(potential_scale),
+                      (C.c_double * 3)(*light), int(shadow_steps), 1 if show_potential else 0,
+                      1 if float_output else 0)
 
 
 def load(path: str | os.PathLike | None = None):
@@ -143,6 +165,8 @@ def load(path: str | os.PathLike | None = None):
         "wfs_batch_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "wfs_observe_noalloc": ([vp, i32, C.POINTER(i32), dp, C.POINTER(Box), i32, C.POINTER(Box), dp, vp], C.c_int),
         "wfs_plane_current": ([vp, dp, dp, dp, C.POINTER(i32), dbl, dp, vp, i32], C.c_int),
+        "wfs_render": ([vp, C.POINTER(RenderDesc), vp, i32], C.c_int),
+        "wfs_render_volume": ([vp, i32, C.POINTER(i32), vp, C.POINTER(RenderDesc), vp, vp], C.c_int),
         # surrogate kernels (include/wfs_fno.h); every pointer is a device pointer
         "wfs_fno_pointwise": ([vp, i32, vp, vp, vp, vp, vp, vp, i32, i32, i64, i32, vp], C.c_int),
         "wfs_fno_pointwise_backward": ([vp, vp, vp, i32, vp, vp, vp, i32, i32, i32, i64, vp], C.c_int),
@@ -379,6 +403,15 @@ class Engine:
         self._ck(self.lib.wfs_plane_current(self.h, _d3(center), _d3(normal), (C.c_double * 2)(*map(float, size)), cnt,
                                             float(mass), C.byref(flux), dens.ctypes.data if dens is not None else None, 0))
         return (flux.value, dens) if density else flux.value
+
+    def render(self, desc: "RenderDesc | None" = None, **kw) -> np.ndarray:
+        """Ray-marched image of psi (and V) as an (height, width, 4) uint8 RGBA array, or
+        float32 when desc.format is 1; keyword arguments build the desc (render_desc)."""
+        d = desc if desc is not None else render_desc(**kw)
+        dtype = np.float32 if d.format == 1 else np.uint8
+        img = np.empty((d.height, d.width, 4), dtype=dtype)
+        self._ck(self.lib.wfs_render(self.h, C.byref(d), img.ctypes.data, 0))
+        return img
 
     def norm(self) -> float:
         v = C.c_double()

@@ -1018,6 +1018,29 @@ int wfs_plane_current(wfs_handle* h, const double center[3], const double normal
     return WFS_OK;
 }
 
+int wfs_render(wfs_handle* h, const wfs_render_desc* desc, void* image, int32_t to_device) {
+    if (!h) return dispatch_err(h);
+    if (!desc || !image) return set_err(h, WFS_ERR_ARG, "invalid argument");
+    if (desc->format != 0 && desc->format != 1) return set_err(h, WFS_ERR_ARG, "format must be 0 (RGBA8) or 1 (float)");
+    if (desc->width < 1 || desc->height < 1 || int64_t(desc->width) * desc->height > (int64_t(1) << 28))
+        return set_err(h, WFS_ERR_ARG, "invalid image size");
+    if (desc->shadow_steps < 0 || desc->shadow_steps > 1000) return set_err(h, WFS_ERR_ARG, "shadow_steps must be in 0..1000");
+    int rc = is_dbl(h) ? to_real<double>(h) : to_real<float>(h);
+    if (rc) return rc;
+    const size_t bytes = size_t(desc->width) * desc->height * (desc->format == 1 ? 16 : 4);
+    void* dst = image;
+    if (!to_device) CK(cudaMalloc(&dst, bytes));
+    const int n[3] = {h->n[0], h->n[1], h->n[2]};
+    cudaError_t e = is_dbl(h) ? launch_render<double>((const Cx<double>*)h->psi, (const float2*)h->V, n, *desc, dst, h->stream)
+                              : launch_render<float>((const Cx<float>*)h->psi, (const float2*)h->V, n, *desc, dst, h->stream);
+    if (e == cudaSuccess && !to_device) e = cudaMemcpyAsync(image, dst, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (!to_device) cudaFree(dst);
+    if (e == cudaErrorInvalidValue) return set_err(h, WFS_ERR_ARG, "invalid camera or step");
+    if (e != cudaSuccess) return set_err(h, WFS_ERR_CUDA, std::string("render: ") + cudaGetErrorString(e));
+    return WFS_OK;
+}
+
 int wfs_norm(wfs_handle* h, double* norm_out) {
     if (!h) return dispatch_err(h);
     if (!norm_out) return set_err(h, WFS_ERR_ARG, "null output");

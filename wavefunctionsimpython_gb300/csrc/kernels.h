@@ -124,6 +124,21 @@ template <typename R>
 cudaError_t launch_plane_current(const Cx<R>* psi, const PlaneCurrentArgs& a, double* partials, int max_blocks,
                                  R* density, cudaStream_t s, int* grid_out);
 
+// ---- headless volume rendering (render.cu) ----
+struct RenderArgs {
+    float eye[3], forward[3], right[3], up[3], light[3];
+    int npad[3];          // padded volume dimensions (axis 0, 1, 2)
+    float tan_half_fov, aspect, step, color_density, atten_density;
+    int width, height, shadow_steps, format;
+    void* out;
+};
+}  // namespace wfs
+struct wfs_render_desc;
+namespace wfs {
+template <typename R>
+cudaError_t launch_render(const Cx<R>* psi, const float2* V, const int n[3], const wfs_render_desc& d, void* out,
+                          cudaStream_t s);
+
 // ---- power series (taylor.cu) ----
 template <typename R>
 struct TaylorArgs {

@@ -153,6 +153,18 @@ class MeasurementTools:
         self.__expected_location = None
         self.__volumetric_requested = bool(try_read_param(config, "measurement.volumetric.enable_animation", False)
                                            or try_read_param(config, "measurement.volumetric.enable_image", False))
+        # sources/measurement.py:521-535: headless frames instead of the vispy canvas (animation not written)
+        self.__enable_volumetric_image = bool(try_read_param(config, "measurement.volumetric.enable_image", False))
+        self.__volumetric_image_capture_interval = int(
+            try_read_param(config, "measurement.volumetric.image_capture_iteration_interval", 100))
+        self.__volumetric = None
+        if self.__enable_volumetric_image:
+            from .volumetric_visualization import VolumetricVisualization
+
+            self.__volumetric = VolumetricVisualization(
+                sim_state._make_engine(),
+                cam_rotation_speed=try_read_param(config, "measurement.volumetric.camera_rotation_speed", 0.0),
+                azimuth=try_read_param(config, "measurement.volumetric.camera_azimuth", 0.0))
         for conf in try_read_param(config, "measurement.volume_probabilities", []):
             v = VolumeProbability(conf, sim_state)
             self._resolve_naming_conflicts(self.__volume_probabilities, v)
@@ -193,7 +205,8 @@ class MeasurementTools:
 
     def fusable(self) -> bool:
         """True when every enabled measurement is computed by the fused device loop."""
-        return (len(self.active_plane_currents()) == 0 and len(self.active_volume_probabilities()) <= 8)
+        return (len(self.active_plane_currents()) == 0 and len(self.active_volume_probabilities()) <= 8
+                and self.__volumetric is None)
 
     def observation_request(self):
         boxes = [v.box for v in self.active_volume_probabilities()]
@@ -220,9 +233,13 @@ class MeasurementTools:
             os.path.join(out, "wave_function_raw", f"wave_function_{iter_data.i:06d}.bin"))
 
     def measure_and_render(self, sim_state: SimState, iter_data: IterData):
-        """sources/measurement.py:644-705 (rendering is not part of this package)."""
+        """sources/measurement.py:644-705; volumetric frames are ray-marched on the GPU
+        (volumetric_visualization.py), plots are not drawn."""
         if sim_state.is_wave_function_saving():
             self.write_wave_function_to_file(sim_state, iter_data)
+        if self.__volumetric is not None and iter_data.i % self.__volumetric_image_capture_interval == 0:
+            self.__volumetric.update(iter_data.i, sim_state.get_delta_time_h_bar_per_hartree())
+            self.__volumetric.render_to_png(sim_state.get_output_dir(), iter_data.i)
         boxes, loc = self.observation_request()
         if boxes or loc is not None:
             probs, er, er2 = sim_state.engine.observe(boxes, loc)
