@@ -1,0 +1,158 @@
+"""Checks at the workloads' own sizes (GPU only): the 64^3 complex128 barrier series
+against the FP64 oracle, the 128^3 power-series oscillator against the analytic
+<x>(t) and the split step, the 256^3 double slit against the FP64 oracle plus
+size-independent properties (unitarity, time reversal, linearity), and every
+instance of the 256-instance batched sweep."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import wfs_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.complex128)
+    b = np.asarray(b, np.complex128)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def scipy_fft():
+    import scipy.fft as sf
+
+    w = os.cpu_count() or 1
+    return (lambda a, norm: sf.fftn(a, norm=norm, workers=w), lambda a, norm: sf.ifftn(a, norm=norm, workers=w))
+
+
+def engine_for(sc, V=None):
+    from wavefunctionsimpython_gb300 import Engine
+
+    e = Engine(sc.n, sc.extent, double_precision=sc.double_precision)
+    e.set_potential(sc.potential() if V is None else V)
+    e.init_gaussian(sc.sigma, sc.r0, sc.k0)
+    return e
+
+
+def test_barrier_64_c128_series_matches_fp64_oracle():
+    """64^3 over 60 Bohr, complex128, 1 Ha barrier, dt 0.01, 200 steps, norm / <r> / <r^2> every 10."""
+    sc = orc.config1_barrier_64()
+    e = engine_for(sc)
+    box = ((0, 0, 0), (63, 63, 63))
+    ps, ls = e.run_split(200, sc.dt, 1.0, 10, [box], box)
+    V = sc.potential()
+    psi = sc.psi0()
+    for k in range(20):
+        assert abs(ps[k, 0] - orc.volume_probability(psi, sc.dx, *box)) < 1e-9
+        rr, rr2 = orc.expected_location(psi, sc.dx, *box)
+        np.testing.assert_allclose(ls[k, :3], rr, rtol=1e-9, atol=1e-10)
+        np.testing.assert_allclose(ls[k, 3:], rr2, rtol=1e-9, atol=1e-10)
+        psi = orc.split_step(psi, V, sc.dx, sc.dt, 1.0, nsteps=10)
+    assert rel(e.get_psi(), psi) < 1e-11
+
+
+def test_oscillator_128_power_series_follows_ehrenfest():
+    """128^3 over 40 Bohr, complex64, omega 0.5, Taylor p=10 with the 4th-order Laplacian,
+    dt 0.005, 1000 steps: <x>(t) = x0 cos(omega t) exactly for a harmonic potential, which
+    the spectral split step follows to 2e-2 Bohr; the power series' finite-difference
+    Laplacian (dispersion error ~(k dx)^4 / 90 at the packet's k dx ~ 0.8) stays within
+    0.1 Bohr of both; the norm is kept."""
+    sc = orc.config2_ho_128()
+    box = ((0, 0, 0), (127, 127, 127))
+    taylor, split = engine_for(sc), engine_for(sc)
+    n0 = taylor.norm()
+    taylor.step_taylor(1000, sc.dt, 1.0, 10, 4)
+    split.step_split(1000, sc.dt, 1.0)
+    x_t = taylor.observe((), box)[1][0]
+    x_s = split.observe((), box)[1][0]
+    x_exact = sc.r0[0] * math.cos(0.5 * 1000 * sc.dt)
+    assert abs(x_s - x_exact) < 2e-2, (x_s, x_exact)
+    assert abs(x_t - x_exact) < 0.1, (x_t, x_exact)
+    assert abs(x_t - x_s) < 0.1
+    assert abs(taylor.norm() / n0 - 1.0) < 1e-4
+
+
+@pytest.fixture(scope="module")
+def slit():
+    return orc.config3_double_slit(256, 80.0)
+
+
+def test_double_slit_256_two_steps_match_fp64_oracle(slit):
+    e = engine_for(slit)
+    e.step_split(2, slit.dt, 1.0)
+    ref = orc.split_step(slit.psi0().astype(np.complex128), slit.potential().astype(np.complex128), slit.dx, slit.dt,
+                         1.0, nsteps=2, double_precision=True, fft=scipy_fft())
+    assert rel(e.get_psi(), ref) < 1e-5
+
+
+def test_double_slit_256_unitarity_and_time_reversal(slit):
+    """Without the absorber V is real: the step is unitary and dt -> -dt undoes it."""
+    V = np.zeros(slit.n, np.complex64)
+    orc.add_potential_wall(V, slit.dx, slit.walls[0])
+    e = engine_for(slit, V)
+    psi0 = e.get_psi()
+    n0 = e.norm()
+    e.step_split(200, slit.dt, 1.0)
+    assert abs(e.norm() / n0 - 1.0) < 1e-4
+    e.step_split(200, -slit.dt, 1.0)
+    assert rel(e.get_psi(), psi0) < 2e-4
+
+
+def test_double_slit_256_linearity(slit):
+    from wavefunctionsimpython_gb300 import Engine
+
+    V = slit.potential()
+    p1 = slit.psi0()
+    p2 = orc.gaussian_wave_packet(slit.n, slit.dx, (2.0,) * 3, (-15.0, 4.0, 0.0), (1.5, -0.5, 0.0), False)
+    a, b = 0.6, 0.8j
+    outs = []
+    for p in (p1, p2, (a * p1 + b * p2).astype(np.complex64)):
+        e = Engine(slit.n, slit.extent)
+        e.set_potential(V)
+        e.set_psi(p)
+        e.step_split(20, slit.dt, 1.0)
+        outs.append(e.get_psi())
+        e.close()
+    assert rel(outs[2], a * outs[0].astype(np.complex128) + b * outs[1]) < 1e-5
+
+
+def test_batched_sweep_full_mix():
+    """The 256-instance sweep (128x32^3, 64x48^3, 48x64^3, 16x96^3) for 500 steps: two
+    instances of every size agree with the single-grid engine, and every instance keeps
+    its norm (barriers only, no absorber), both to 5e-4: 500 complex64 steps accumulate
+    FP32 rounding beyond the 1e-5 bar that short runs meet against the FP64 oracle."""
+    from wavefunctionsimpython_gb300 import Engine
+    from wavefunctionsimpython_gb300._lib import Batch
+
+    mix = [(32, 128), (48, 64), (64, 48), (96, 16)]
+    sizes = [n for n, c in mix for _ in range(c)]
+    rng = np.random.default_rng(2024)
+    L = 40.0
+    b = Batch(sizes, [L] * len(sizes))
+    params = []
+    for i, n in enumerate(sizes):
+        U, w = rng.uniform(0.2, 2.0), rng.uniform(1.0, 4.0)
+        k0, sig, x0 = rng.uniform(0.5, 3.0), rng.uniform(1.0, 3.0), rng.uniform(-12.0, -6.0)
+        b.add_wall(i, U, (0, 0, 0), (1, 0, 0), w)
+        b.init_gaussian(i, (sig,) * 3, (x0, 0, 0), (k0, 0, 0))
+        params.append((U, w, k0, sig, x0))
+    norms0 = [float(np.sum(np.abs(b.get_psi(i).astype(np.complex128)) ** 2)) for i in range(len(sizes))]
+    b.run(500, 0.01, 1.0, graph=True)
+    b.synchronize()
+    for i in range(len(sizes)):
+        n1 = float(np.sum(np.abs(b.get_psi(i).astype(np.complex128)) ** 2))
+        assert abs(n1 / norms0[i] - 1.0) < 5e-4, i
+    first = {}
+    for i, n in enumerate(sizes):
+        first.setdefault(n, []).append(i)
+    for n, idx in first.items():
+        for i in (idx[0], idx[-1]):
+            U, w, k0, sig, x0 = params[i]
+            e = Engine((n,) * 3, (L,) * 3)
+            e.add_wall(U, (0, 0, 0), (1, 0, 0), w)
+            e.init_gaussian((sig,) * 3, (x0, 0, 0), (k0, 0, 0))
+            e.step_split(500, 0.01, 1.0)
+            assert rel(b.get_psi(i), e.get_psi()) < 5e-4, (n, i)
+            e.close()
