@@ -156,3 +156,28 @@ def test_batched_sweep_full_mix():
             e.step_split(500, 0.01, 1.0)
             assert rel(b.get_psi(i), e.get_psi()) < 5e-4, (n, i)
             e.close()
+
+
+@pytest.mark.parametrize("n", [512, 1024])
+def test_maximum_sizes_keep_norm_and_reverse(n):
+    """The largest grids: 512^3 (fused plane pass) and 1024^3 (per-axis passes, 8 GiB psi
+    plus V and the phase table) keep the norm with a real barrier and return to the
+    initial <r>, <r^2> after dt -> -dt; everything stays on the device."""
+    from wavefunctionsimpython_gb300 import Engine
+
+    L = 80.0
+    e = Engine((n,) * 3, (L,) * 3)
+    e.add_wall(5.0, (0.0, 0.0, 0.0), (1.0, 0.0, 0.0), 1.0)
+    e.init_gaussian((3.0,) * 3, (-10.0, 1.0, 0.0), (2.0, 0.0, 0.5))
+    box = ((1, 1, 1), (n - 3, n - 3, n - 3))
+    n0 = e.norm()
+    _, r0, q0 = e.observe((), box)
+    e.step_split(10, 0.01, 1.0)
+    _, r1, _ = e.observe((), box)
+    assert abs(r1[0] - r0[0]) > 0.1          # the packet moved
+    assert abs(e.norm() / n0 - 1.0) < 1e-5
+    e.step_split(10, -0.01, 1.0)
+    _, r2, q2 = e.observe((), box)
+    np.testing.assert_allclose(r2, r0, atol=1e-4)
+    np.testing.assert_allclose(q2, q0, rtol=1e-4)
+    e.close()
