@@ -30,7 +30,7 @@ struct InstDesc {
     Cx<float>* psi;
     const Cx<float>* ephase;
     const Cx<float>* kin;   // [half x][half y][half z][full x][full y][full z], L each
-    const Cx<float>* tw;    // L roots
+    const Cx<float>* tw;    // two-stage twiddle table (3L entries, two_stage_roots)
     int L;
 };
 
@@ -64,7 +64,7 @@ __device__ __forceinline__ void x_kin_tile(const InstDesc& in, int tile, const C
     auto sf = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
     auto si = [&](int k2, int n1) { return (k2 * Q + n1) * W + c; };
     const int tt = in_block ? t : T;
-    two_stage<P, Q, -1, float>(a1, a2, sm, in.tw, tt, sf);
+    two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(in.tw), tt, sf);
     if (tt < Q) {
         Cx<float> cf = mk<float>(0.f, 0.f);
         if (active) cf = scale(cmul(k3[L + col / L], k3[2 * L + col % L]), 1.0f / float(L));
@@ -72,7 +72,7 @@ __device__ __forceinline__ void x_kin_tile(const InstDesc& in, int tile, const C
         for (int k = 0; k < P; ++k) a2[k] = cmul(a2[k], cmul(k3[t + Q * k], cf));
     }
     __syncthreads();
-    two_stage<Q, P, +1, float>(a2, a1, sm, in.tw, tt, si);
+    two_stage<Q, P, +1, TW_ROW>(a2, a1, sm, tw_rows<Q, P, P, Q>(in.tw), tt, si);
     if (active && t < P) {
 #pragma unroll
         for (int i = 0; i < Q; ++i) st_l2<float>(base + int64_t(t + P * i) * plane, a1[i]);
@@ -96,7 +96,7 @@ __device__ __forceinline__ void z_plain_tile(const InstDesc& in, int tile, Cx<fl
     }
     auto sf = [&](int k2, int n1) { return r * RS + k2 * (P + 1) + n1; };
     const int tt = in_block ? t : T;
-    two_stage<P, Q, SIGN, float>(a1, a2, sm, in.tw, tt, sf);
+    two_stage<P, Q, SIGN, TW_ANGLE>(a1, a2, sm, in.tw, tt, sf);
     const float sc = rsqrtf(float(L));
     if (active && t < Q) {
 #pragma unroll
@@ -202,7 +202,7 @@ struct wfs_batch {
     Cx<float>* ephase;
     Cx<float>* kin;               // 6 L per instance
     std::vector<int64_t> kin_off;
-    Cx<float>* tw;                // roots per distinct L
+    Cx<float>* tw;                // two-stage twiddle tables per distinct L
     std::map<int, int64_t> tw_off;
     InstDesc* dinst;
     int* dorder;
@@ -416,8 +416,8 @@ int wfs_batch_create(const wfs_batch_desc* d, wfs_batch** out) {
     for (int v : sorted)
         if (!b->tw_off.count(v)) {
             b->tw_off[v] = int64_t(roots.size());
-            roots.resize(roots.size() + v);
-            roots_table<float>(v, roots.data() + b->tw_off[v]);
+            roots.resize(roots.size() + 3 * v);
+            two_stage_roots<float>(v, roots.data() + b->tw_off[v]);
         }
     e = cudaMalloc(&b->tw, roots.size() * sizeof(Cx<float>));
     if (e == cudaSuccess) e = cudaMemcpy(b->tw, roots.data(), roots.size() * sizeof(Cx<float>), cudaMemcpyHostToDevice);

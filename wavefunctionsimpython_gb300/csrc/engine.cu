@@ -141,13 +141,10 @@ int ensure_partials(wfs_handle* h, size_t need) {
 template <typename R>
 int upload_roots(wfs_handle* h, int axis) {
     const int L = h->n[axis];
-    std::vector<Cx<R>> t(L);
-    for (int m = 0; m < L; ++m) {
-        const double a = -2.0 * M_PI * double(m) / double(L);
-        t[m] = mk<R>(R(std::cos(a)), R(std::sin(a)));
-    }
-    CK(cudaMalloc(&h->tw[axis], L * sizeof(Cx<R>)));
-    CK(cudaMemcpy(h->tw[axis], t.data(), L * sizeof(Cx<R>), cudaMemcpyHostToDevice));
+    std::vector<Cx<R>> t(3 * size_t(L));
+    if (!two_stage_roots<R>(L, t.data())) return WFS_ERR_UNSUPPORTED;
+    CK(cudaMalloc(&h->tw[axis], t.size() * sizeof(Cx<R>)));
+    CK(cudaMemcpy(h->tw[axis], t.data(), t.size() * sizeof(Cx<R>), cudaMemcpyHostToDevice));
     return WFS_OK;
 }
 

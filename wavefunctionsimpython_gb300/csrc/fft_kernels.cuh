@@ -17,6 +17,7 @@
 // gives each CTA W whole rows.
 #pragma once
 
+#include <cmath>
 #include <cstdlib>
 
 #include "kernels.h"
@@ -26,15 +27,39 @@ namespace wfs {
 // Two-stage transform. in: thread t < P1 holds x[t + P1*i] in a_in[Q1].
 // out: thread t < Q1 holds X[t + Q1*k] in a_out[P1]. SIGN -1 forward, +1 inverse.
 // sidx(k2, n1) is the shared-memory slot of A[n1][k2] for this thread's pencil.
-template <int P1, int Q1, int SIGN, typename R, typename SI>
+// Twiddles w = exp(-2 pi i t k2 / L) come from the axis table (two_stage_roots) in one
+// of two orders, whichever suits how the kernel maps pencils onto a warp:
+//   TW_ANGLE: tw[t*k2] (tw = the table itself); a warp that spans many t (rows of
+//             a contiguous axis) finds the small angles of each k2 in a few lines;
+//   TW_ROW:   tw[t*Q1 + k2] (tw = the plan's row block); a warp that spans one or
+//             two t (strided axes) reads its contiguous row, two twiddles per 16 bytes.
+constexpr int TW_ANGLE = 0, TW_ROW = 1;
+// Row block of the plan (P1, Q1) in an axis table whose own plan is (P, Q).
+template <int P1, int Q1, int P, int Q, typename R>
+__device__ __forceinline__ const Cx<R>* tw_rows(const Cx<R>* tw) {
+    return tw + (P1 == P ? 1 : 2) * (P * Q);
+}
+template <int P1, int Q1, int SIGN, int TWL, typename R, typename SI>
 __device__ __forceinline__ void two_stage(Cx<R> (&a_in)[Q1], Cx<R> (&a_out)[P1], Cx<R>* sm,
                                           const Cx<R>* __restrict__ tw, int t, SI sidx) {
     if (t < P1) {
         dft<Q1, SIGN, R>(a_in);
+        auto apply = [&](int k2, Cx<R> w) { a_in[k2] = (SIGN < 0) ? cmul(a_in[k2], w) : cmulc(a_in[k2], w); };
+        if constexpr (TWL == TW_ROW && sizeof(Cx<R>) == 8 && Q1 % 2 == 0) {
+            const Cx<R>* row = tw + t * Q1;
 #pragma unroll
-        for (int k2 = 1; k2 < Q1; ++k2) {
-            Cx<R> w = tw[t * k2];
-            a_in[k2] = (SIGN < 0) ? cmul(a_in[k2], w) : cmulc(a_in[k2], w);
+            for (int j = 0; j < Q1 / 2; ++j) {
+                const float4 w2 = __ldg(reinterpret_cast<const float4*>(row) + j);
+                if (j > 0) apply(2 * j, mk<R>(w2.x, w2.y));
+                apply(2 * j + 1, mk<R>(w2.z, w2.w));
+            }
+        } else if constexpr (TWL == TW_ROW) {
+            const Cx<R>* row = tw + t * Q1;
+#pragma unroll
+            for (int k2 = 1; k2 < Q1; ++k2) apply(k2, row[k2]);
+        } else {
+#pragma unroll
+            for (int k2 = 1; k2 < Q1; ++k2) apply(k2, tw[t * k2]);
         }
 #pragma unroll
         for (int k2 = 0; k2 < Q1; ++k2) sm[sidx(k2, t)] = a_in[k2];
@@ -190,14 +215,14 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_strided_ker
     auto sidx_i = [&](int k2, int n1) { return (k2 * Q + n1) * W + c; };
 
     if constexpr (OP == OP_PLAIN) {
-        if (a.dir < 0) two_stage<P, Q, -1, R>(a1, a2, sm, a.tw, t, sidx_f);
-        else two_stage<P, Q, +1, R>(a1, a2, sm, a.tw, t, sidx_f);
+        if (a.dir < 0) two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
+        else two_stage<P, Q, +1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
         if (active && t < Q) {
 #pragma unroll
             for (int k = 0; k < P; ++k) base[(t + Q * k) * rs] = scale(a2[k], a.scale);
         }
     } else {  // OP_KIN: forward, diagonal kinetic factor, inverse
-        two_stage<P, Q, -1, R>(a1, a2, sm, a.tw, t, sidx_f);
+        two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
         if (t < Q) {
             Cx<R> cf = mk<R>(R(0), R(0));
             if (active) cf = scale(cmul(a.k_c1[col / a.c2n], a.k_c2[col % a.c2n]), a.scale);
@@ -205,7 +230,7 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_strided_ker
             for (int k = 0; k < P; ++k) a2[k] = cmul(a2[k], cmul(a.k_row[t + Q * k], cf));
         }
         __syncthreads();
-        two_stage<Q, P, +1, R>(a2, a1, sm, a.tw, t, sidx_i);
+        two_stage<Q, P, +1, TW_ROW>(a2, a1, sm, tw_rows<Q, P, P, Q>(a.tw), t, sidx_i);
         if (active && t < P) {
 #pragma unroll
             for (int i = 0; i < Q; ++i) base[(t + P * i) * rs] = a1[i];
@@ -279,14 +304,14 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS)
             for (int i = 0; i < Q; ++i) a1[i] = active ? src[(t + P * i) * W] : mk<R>(R(0), R(0));
         }
         if constexpr (OP == OP_PLAIN) {
-            if (a.dir < 0) two_stage<P, Q, -1, R>(a1, a2, sm, a.tw, t, sidx_f);
-            else two_stage<P, Q, +1, R>(a1, a2, sm, a.tw, t, sidx_f);
+            if (a.dir < 0) two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
+            else two_stage<P, Q, +1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
             if (active && t < Q) {
 #pragma unroll
                 for (int k = 0; k < P; ++k) base[(t + Q * k) * rs] = scale(a2[k], a.scale);
             }
         } else {  // OP_KIN
-            two_stage<P, Q, -1, R>(a1, a2, sm, a.tw, t, sidx_f);
+            two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
             if (t < Q) {
                 Cx<R> cf = mk<R>(R(0), R(0));
                 if (active) cf = scale(cmul(a.k_c1[col / a.c2n], a.k_c2[col % a.c2n]), a.scale);
@@ -294,7 +319,7 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS)
                 for (int k = 0; k < P; ++k) a2[k] = cmul(a2[k], cmul(a.k_row[t + Q * k], cf));
             }
             __syncthreads();
-            two_stage<Q, P, +1, R>(a2, a1, sm, a.tw, t, sidx_i);
+            two_stage<Q, P, +1, TW_ROW>(a2, a1, sm, tw_rows<Q, P, P, Q>(a.tw), t, sidx_i);
             if (active && t < P) {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) base[(t + P * i) * rs] = a1[i];
@@ -329,14 +354,14 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_contig_kern
     auto sidx_i = [&](int k2, int n1) { return r * RS + k2 * (Q + 1) + n1; };
 
     if constexpr (OP == OP_PLAIN) {
-        if (a.dir < 0) two_stage<P, Q, -1, R>(a1, a2, sm, a.tw, t, sidx_f);
-        else two_stage<P, Q, +1, R>(a1, a2, sm, a.tw, t, sidx_f);
+        if (a.dir < 0) two_stage<P, Q, -1, TW_ANGLE>(a1, a2, sm, a.tw, t, sidx_f);
+        else two_stage<P, Q, +1, TW_ANGLE>(a1, a2, sm, a.tw, t, sidx_f);
         if (active && t < Q) {
 #pragma unroll
             for (int k = 0; k < P; ++k) rp[t + Q * k] = scale(a2[k], a.scale);
         }
     } else if constexpr (OP == OP_VPH) {  // inverse, potential phase, forward
-        two_stage<P, Q, +1, R>(a1, a2, sm, a.tw, t, sidx_f);
+        two_stage<P, Q, +1, TW_ANGLE>(a1, a2, sm, a.tw, t, sidx_f);
         if (t < Q) {
             const Cx<R>* ep = a.ephase + row * L;
 #pragma unroll
@@ -346,13 +371,13 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_contig_kern
             }
         }
         __syncthreads();
-        two_stage<Q, P, -1, R>(a2, a1, sm, a.tw, t, sidx_i);
+        two_stage<Q, P, -1, TW_ANGLE>(a2, a1, sm, a.tw, t, sidx_i);
         if (active && t < P) {
 #pragma unroll
             for (int i = 0; i < Q; ++i) rp[t + P * i] = a1[i];
         }
     } else {  // OP_OBS: inverse transform in registers, observe, no store
-        two_stage<P, Q, +1, R>(a1, a2, sm, a.tw, t, sidx_f);
+        two_stage<P, Q, +1, TW_ANGLE>(a1, a2, sm, a.tw, t, sidx_f);
         R acc[kMaxBox + kLocQ];
 #pragma unroll
         for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = R(0);
@@ -378,26 +403,9 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_contig_kern
 template <int L>
 struct PlanOf;
 #define WFS_PLAN(L_, P_, Q_) template <> struct PlanOf<L_> { static constexpr int P = P_, Q = Q_; };
-WFS_PLAN(2, 2, 1)
-WFS_PLAN(3, 3, 1)
-WFS_PLAN(4, 2, 2)
-WFS_PLAN(6, 3, 2)
-WFS_PLAN(8, 4, 2)
-WFS_PLAN(12, 4, 3)
-WFS_PLAN(16, 4, 4)
-WFS_PLAN(24, 6, 4)
-WFS_PLAN(32, 8, 4)
-WFS_PLAN(48, 8, 6)
-WFS_PLAN(64, 8, 8)
-WFS_PLAN(96, 12, 8)
-WFS_PLAN(128, 16, 8)
-WFS_PLAN(192, 16, 12)
-WFS_PLAN(256, 16, 16)
-WFS_PLAN(384, 24, 16)
-WFS_PLAN(512, 32, 16)
-WFS_PLAN(768, 32, 24)
-WFS_PLAN(1024, 32, 32)
+WFS_PLAN_LIST(WFS_PLAN)
 #undef WFS_PLAN
+
 
 template <typename R, int T>
 struct StridedW {

@@ -555,11 +555,11 @@ const Cx<float>* twiddles_for(int N) {
     std::lock_guard<std::mutex> lk(g_fno_mu);
     auto it = g_twiddles.find({dev, N});
     if (it != g_twiddles.end()) return it->second;
-    std::vector<Cx<float>> t(N);
-    roots_table<float>(N, t.data());
+    std::vector<Cx<float>> t(3 * size_t(N));
+    if (!two_stage_roots<float>(N, t.data())) return nullptr;
     Cx<float>* d = nullptr;
-    if (cudaMalloc(&d, N * sizeof(Cx<float>)) != cudaSuccess) return nullptr;
-    if (cudaMemcpy(d, t.data(), N * sizeof(Cx<float>), cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (cudaMalloc(&d, t.size() * sizeof(Cx<float>)) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, t.data(), t.size() * sizeof(Cx<float>), cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(d);
         return nullptr;
     }

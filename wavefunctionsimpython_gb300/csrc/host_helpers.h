@@ -153,12 +153,24 @@ inline void kinetic_axis(int L, double dx, double dt, double mass, double frac, 
     }
 }
 
+// Twiddle table of a length-L axis in both orders two_stage reads (3L entries):
+// [0, L) out[m] = exp(-2 pi i m / L); [L, 2L) the (P, Q) plan's rows
+// out[L + t*Q + k2] = exp(-2 pi i t k2 / L) (t < P, k2 < Q); [2L, 3L) the transposed
+// (Q, P) plan's rows. False for unsupported L.
 template <typename R>
-inline void roots_table(int L, Cx<R>* out) {
-    for (int m = 0; m < L; ++m) {
-        const double a = -2.0 * M_PI * double(m) / double(L);
-        out[m] = mk<R>(R(std::cos(a)), R(std::sin(a)));
-    }
+inline bool two_stage_roots(int L, Cx<R>* out) {
+    int P = 0, Q = 0;
+    if (!plan_pq(L, P, Q)) return false;
+    auto root = [&](int m) {
+        const double a = -2.0 * 3.14159265358979323846 * double(m % L) / double(L);
+        return mk<R>(R(std::cos(a)), R(std::sin(a)));
+    };
+    for (int m = 0; m < L; ++m) out[m] = root(m);
+    for (int t = 0; t < P; ++t)
+        for (int k = 0; k < Q; ++k) out[L + t * Q + k] = root(t * k);
+    for (int t = 0; t < Q; ++t)
+        for (int k = 0; k < P; ++k) out[2 * L + t * P + k] = root(t * k);
+    return true;
 }
 
 }  // namespace wfs

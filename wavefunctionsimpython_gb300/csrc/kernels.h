@@ -20,6 +20,23 @@
 
 namespace wfs {
 
+// Two-stage plans (L = P * Q) of the supported FFT lengths.
+#define WFS_PLAN_LIST(M)                                                                                      \
+    M(2, 2, 1) M(3, 3, 1) M(4, 2, 2) M(6, 3, 2) M(8, 4, 2) M(12, 4, 3) M(16, 4, 4) M(24, 6, 4) M(32, 8, 4)      \
+    M(48, 8, 6) M(64, 8, 8) M(96, 12, 8) M(128, 16, 8) M(192, 16, 12) M(256, 16, 16) M(384, 24, 16)            \
+    M(512, 32, 16) M(768, 32, 24) M(1024, 32, 32)
+
+// (P, Q) of the two-stage plan of length L on the host; false for unsupported lengths.
+inline bool plan_pq(int L, int& P, int& Q) {
+    switch (L) {
+#define WFS_PLAN(L_, P_, Q_) case L_: P = P_; Q = Q_; return true;
+        WFS_PLAN_LIST(WFS_PLAN)
+#undef WFS_PLAN
+        default: return false;
+    }
+}
+
+
 constexpr int kMaxBox = 8;      // volume-probability boxes per fused observation
 constexpr int kLocQ = 7;        // location box sums: S, Sx, Sy, Sz, Sxx, Syy, Szz
 
@@ -48,7 +65,7 @@ struct ObsArgs {
 template <typename R>
 struct PassArgs {
     Cx<R>* data;
-    const Cx<R>* tw;        // tw[m] = exp(-2 pi i m / L), m < L
+    const Cx<R>* tw;        // twiddle table of the axis (two_stage_roots: 3L entries)
     int64_t outer_stride;
     int64_t row_stride;
     int32_t ncols;          // strided: columns per outer slab

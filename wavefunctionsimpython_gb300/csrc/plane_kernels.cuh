@@ -80,7 +80,7 @@ __device__ __forceinline__ void plane_y_tile(Cx<R>* plane, int nz, int tile, con
         for (int i = 0; i < Q; ++i) a1[i] = active ? ld_l2<R>(base + int64_t(t + P * i) * nz) : mk<R>(R(0), R(0));
     }
     auto sidx = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
-    two_stage<P, Q, SIGN, R>(a1, a2, sm, tw, in_block ? t : T, sidx);
+    two_stage<P, Q, SIGN, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(tw), in_block ? t : T, sidx);
     if (active && t < Q) {
 #pragma unroll
         for (int k = 0; k < P; ++k) st_l2<R>(base + int64_t(t + Q * k) * nz, scale(a2[k], sc));
@@ -108,7 +108,7 @@ __device__ __forceinline__ void plane_z_tile(Cx<R>* plane, const Cx<R>* eplane, 
     auto sidx_f = [&](int k2, int n1) { return r * RS + k2 * (P + 1) + n1; };
     auto sidx_i = [&](int k2, int n1) { return r * RS + k2 * (Q + 1) + n1; };
     const int tt = in_block ? t : T;
-    two_stage<P, Q, +1, R>(a1, a2, sm, tw, tt, sidx_f);
+    two_stage<P, Q, +1, TW_ANGLE>(a1, a2, sm, tw, tt, sidx_f);
     if (tt < Q) {
 #pragma unroll
         for (int k = 0; k < P; ++k) {
@@ -117,7 +117,7 @@ __device__ __forceinline__ void plane_z_tile(Cx<R>* plane, const Cx<R>* eplane, 
         }
     }
     __syncthreads();
-    two_stage<Q, P, -1, R>(a2, a1, sm, tw, tt, sidx_i);
+    two_stage<Q, P, -1, TW_ANGLE>(a2, a1, sm, tw, tt, sidx_i);
     if (active && t < P) {
 #pragma unroll
         for (int i = 0; i < Q; ++i) st_l2<R>(rp + t + P * i, a1[i]);
