@@ -80,112 +80,29 @@ __device__ __forceinline__ R simpson_w(int v, int b, int cnt) {
     return (j & 1) ? R(4) : R(2);
 }
 
-// Block-wide sum of acc[0..nq) written to partials[blockIdx.x * nq + q].
-// Warp sums use the working precision R (a 32-term tree); the sums of the warps
-// and, later, of the blocks are FP64. FP64 work is a few adds per block.
-template <int NQ, typename R>
-__device__ __forceinline__ void block_reduce_store(R (&acc)[NQ], int nq, double* scratch, double* out) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
+// Observation sums (volume probabilities with Simpson weights, location moments).
+// A thread sums its own elements and a warp its threads in the working precision
+// (short sums); only the sums of warps and, in reduce_partials_kernel, of CTAs are
+// FP64, since GB300's FP64 rate is a small fraction of its FP32 rate. Partials are
+// laid out [CTA][nbox box probabilities, then the 7 location sums].
+//
+// Sums v over the warp in the working precision and stores the sum, as FP64, at
+// scratch[q * 32 + warp]; every lane of the warp must call it.
+template <typename R>
+__device__ __forceinline__ void warp_sum_to(R v, double* scratch, int q) {
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        R v = acc[q];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if (lane == 0 && q < nq) scratch[q * 32 + warp] = double(v);
-    }
-    __syncthreads();
-    if (threadIdx.x < nq) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) scratch[q * 32 + (threadIdx.x >> 5)] = double(v);
+}
+// FP64 sums over the warps of quantities [0, nq) into out[blockIdx.x * nq + q]
+// (after a block barrier that follows the warp_sum_to calls).
+__device__ __forceinline__ void block_partials(const double* scratch, int nq, double* out) {
+    const int nwarp = (blockDim.x + 31) >> 5;
+    if (int(threadIdx.x) < nq) {
         double s = 0.0;
         for (int w = 0; w < nwarp; ++w) s += scratch[threadIdx.x * 32 + w];
         out[(int64_t)blockIdx.x * nq + threadIdx.x] = s;
     }
-}
-
-// Observation sums. A thread sums the few elements of one (x, y) row it holds
-// (RowAcc: Simpson z-weight * |psi|^2 per box, and the location moments in z),
-// folds the row in with the row's x/y weights (obs_row_flush), and the block
-// reduction adds threads in a 32-term tree; all of that is in the working
-// precision. Only warp-to-block and block-to-grid sums are FP64, since GB300's
-// FP64 rate is a small fraction of its FP32 rate.
-template <typename R>
-struct RowAcc {
-    R box[kMaxBox];
-    R s0, sz, szz;
-    __device__ __forceinline__ void zero() {
-#pragma unroll
-        for (int b = 0; b < kMaxBox; ++b) box[b] = R(0);
-        s0 = sz = szz = R(0);
-    }
-};
-
-template <typename R>
-__device__ __forceinline__ void obs_row_element(const ObsArgs& o, RowAcc<R>& ra, int z, Cx<R> v) {
-    const R p = v.x * v.x + v.y * v.y;
-#pragma unroll
-    for (int b = 0; b < kMaxBox; ++b)
-        if (b < o.nbox) ra.box[b] += simpson_w<R>(z, o.box[b].b[2], o.box[b].c[2]) * p;
-    if (o.has_loc) {
-        const R w = simpson_w<R>(z, o.loc.b[2], o.loc.c[2]) * p;
-        const R rz = R(o.dx[2]) * R(z - o.n[2] / 2);
-        ra.s0 += w;
-        ra.sz += w * rz;
-        ra.szz += w * rz * rz;
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ void obs_row_flush(const ObsArgs& o, R (&acc)[kMaxBox + kLocQ], const RowAcc<R>& ra,
-                                              const R (&wxy)[kMaxBox], R lxy, R rx, R ry) {
-#pragma unroll
-    for (int b = 0; b < kMaxBox; ++b)
-        if (b < o.nbox) acc[b] += wxy[b] * ra.box[b];
-    if (o.has_loc && lxy != R(0)) {
-        const R ls0 = lxy * ra.s0;
-        acc[kMaxBox + 0] += ls0;
-        acc[kMaxBox + 1] += rx * ls0;
-        acc[kMaxBox + 2] += ry * ls0;
-        acc[kMaxBox + 3] += lxy * ra.sz;
-        acc[kMaxBox + 4] += rx * rx * ls0;
-        acc[kMaxBox + 5] += ry * ry * ls0;
-        acc[kMaxBox + 6] += lxy * ra.szz;
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ void obs_row_factors(const ObsArgs& o, int x, int y, R (&wxy)[kMaxBox], R& lxy,
-                                                R& rx, R& ry) {
-#pragma unroll
-    for (int b = 0; b < kMaxBox; ++b) {
-        wxy[b] = (b < o.nbox) ? simpson_w<R>(x, o.box[b].b[0], o.box[b].c[0]) *
-                                    simpson_w<R>(y, o.box[b].b[1], o.box[b].c[1])
-                              : R(0);
-    }
-    if (o.has_loc) {
-        lxy = simpson_w<R>(x, o.loc.b[0], o.loc.c[0]) * simpson_w<R>(y, o.loc.b[1], o.loc.c[1]);
-    } else {
-        lxy = R(0);
-    }
-    rx = R(o.dx[0]) * R(x - o.n[0] / 2);
-    ry = R(o.dx[1]) * R(y - o.n[1] / 2);
-}
-
-// Compacts the fixed accumulator layout to [nbox probs][loc sums] and stores per-CTA partials.
-template <typename R>
-__device__ __forceinline__ void obs_store(const ObsArgs& o, R (&acc)[kMaxBox + kLocQ], double* scratch) {
-    R packed[kMaxBox + kLocQ];
-#pragma unroll
-    for (int q = 0; q < kMaxBox + kLocQ; ++q) packed[q] = R(0);
-#pragma unroll
-    for (int b = 0; b < kMaxBox; ++b)
-        if (b < o.nbox) packed[b] = acc[b];
-#pragma unroll
-    for (int q = 0; q < kLocQ; ++q) {
-        // place location sums right after the boxes
-#pragma unroll
-        for (int b = 0; b <= kMaxBox; ++b)
-            if (b == o.nbox && o.has_loc) packed[b + q] = acc[kMaxBox + q];
-    }
-    block_reduce_store<kMaxBox + kLocQ>(packed, o.nq, scratch, o.partials);
 }
 
 // ---------------------------------------------------------------------------
@@ -378,22 +295,53 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_contig_kern
         }
     } else {  // OP_OBS: inverse transform in registers, observe, no store
         two_stage<P, Q, +1, TW_ANGLE>(a1, a2, sm, a.tw, t, sidx_f);
-        R acc[kMaxBox + kLocQ];
+        // |psi|^2 of this thread's elements (z = t + Q*k), then one pass per requested
+        // box over those 16 values: a runtime loop over the boxes keeps the code small
+        // (the fully unrolled form over all kMaxBox boxes missed the instruction cache)
+        const ObsArgs& o = a.obs;
+        const bool own = active && t < Q;
+        const int x = int(row / o.n[1]), y = int(row % o.n[1]);
+        R pk[P];
 #pragma unroll
-        for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = R(0);
-        if (active && t < Q) {
-            const ObsArgs& o = a.obs;
-            const int x = int(row / o.n[1]), y = int(row % o.n[1]);
-            R wxy[kMaxBox], lxy, rx, ry;
-            obs_row_factors<R>(o, x, y, wxy, lxy, rx, ry);
-            RowAcc<R> ra;
-            ra.zero();
+        for (int k = 0; k < P; ++k) {
+            const Cx<R> v = scale(a2[k], a.scale);
+            pk[k] = own ? v.x * v.x + v.y * v.y : R(0);
+        }
+        __syncthreads();  // the transpose scratch is reused for the block sums
+        double* scratch = reinterpret_cast<double*>(smem_raw);
+#pragma unroll 1
+        for (int b = 0; b < o.nbox; ++b) {
+            const ObsBox bx = o.box[b];
+            const R wxy = simpson_w<R>(x, bx.b[0], bx.c[0]) * simpson_w<R>(y, bx.b[1], bx.c[1]);
+            R v = R(0);
+            if (wxy != R(0)) {
+                R sz = R(0);
 #pragma unroll
-            for (int k = 0; k < P; ++k) obs_row_element<R>(o, ra, t + Q * k, scale(a2[k], a.scale));
-            obs_row_flush<R>(o, acc, ra, wxy, lxy, rx, ry);
+                for (int k = 0; k < P; ++k) sz += simpson_w<R>(t + Q * k, bx.b[2], bx.c[2]) * pk[k];
+                v = wxy * sz;
+            }
+            warp_sum_to<R>(v, scratch, b);
+        }
+        if (o.has_loc) {
+            R s0 = R(0), sz = R(0), szz = R(0);
+#pragma unroll
+            for (int k = 0; k < P; ++k) {
+                const int z = t + Q * k;
+                const R w = simpson_w<R>(z, o.loc.b[2], o.loc.c[2]) * pk[k];
+                const R rz = R(o.dx[2]) * R(z - o.n[2] / 2);
+                s0 += w;
+                sz += w * rz;
+                szz += w * rz * rz;
+            }
+            const R lxy = simpson_w<R>(x, o.loc.b[0], o.loc.c[0]) * simpson_w<R>(y, o.loc.b[1], o.loc.c[1]);
+            const R rx = R(o.dx[0]) * R(x - o.n[0] / 2), ry = R(o.dx[1]) * R(y - o.n[1] / 2);
+            const R ls0 = lxy * s0;
+            const R q7[kLocQ] = {ls0, rx * ls0, ry * ls0, lxy * sz, rx * rx * ls0, ry * ry * ls0, lxy * szz};
+#pragma unroll
+            for (int q = 0; q < kLocQ; ++q) warp_sum_to<R>(q7[q], scratch, o.nbox + q);
         }
         __syncthreads();
-        obs_store(a.obs, acc, reinterpret_cast<double*>(smem_raw));
+        block_partials(scratch, o.nq, o.partials);
     }
 }
 

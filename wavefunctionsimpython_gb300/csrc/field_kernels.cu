@@ -365,20 +365,50 @@ __global__ void __launch_bounds__(256) observe_real_kernel(const Cx<R>* __restri
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t nrows = int64_t(o.n[0]) * o.n[1];
     const int64_t row = int64_t(blockIdx.x) * kObsRowsPerCta + warp;
-    R acc[kMaxBox + kLocQ];
-#pragma unroll
-    for (int q = 0; q < kMaxBox + kLocQ; ++q) acc[q] = R(0);
-    if (row < nrows) {
-        const int x = int(row / o.n[1]), y = int(row % o.n[1]);
-        R wxy[kMaxBox], lxy, rx, ry;
-        obs_row_factors<R>(o, x, y, wxy, lxy, rx, ry);
-        const Cx<R>* rp = psi + row * o.n[2];
-        RowAcc<R> ra;
-        ra.zero();
-        for (int z = lane; z < o.n[2]; z += 32) obs_row_element<R>(o, ra, z, rp[z]);
-        obs_row_flush<R>(o, acc, ra, wxy, lxy, rx, ry);
+    const bool own = row < nrows;
+    const int x = own ? int(row / o.n[1]) : 0, y = own ? int(row % o.n[1]) : 0;
+    const Cx<R>* rp = psi + (own ? row : 0) * o.n[2];
+    auto p2 = [&](int z) {
+        const Cx<R> v = rp[z];
+        return v.x * v.x + v.y * v.y;
+    };
+    // one pass per requested box over the z range where its Simpson weight is nonzero
+#pragma unroll 1
+    for (int b = 0; b < o.nbox; ++b) {
+        const ObsBox bx = o.box[b];
+        const R wxy = own ? simpson_w<R>(x, bx.b[0], bx.c[0]) * simpson_w<R>(y, bx.b[1], bx.c[1]) : R(0);
+        R v = R(0);
+        if (wxy != R(0)) {
+            const int z0 = bx.b[2] > 0 ? bx.b[2] : 0;
+            const int z1 = (bx.b[2] + bx.c[2]) < o.n[2] ? (bx.b[2] + bx.c[2]) : o.n[2];
+            R sz = R(0);
+            for (int z = z0 + lane; z < z1; z += 32) sz += simpson_w<R>(z, bx.b[2], bx.c[2]) * p2(z);
+            v = wxy * sz;
+        }
+        warp_sum_to<R>(v, scratch, b);
     }
-    obs_store(o, acc, scratch);
+    if (o.has_loc) {
+        const R lxy = own ? simpson_w<R>(x, o.loc.b[0], o.loc.c[0]) * simpson_w<R>(y, o.loc.b[1], o.loc.c[1]) : R(0);
+        R s0 = R(0), sz = R(0), szz = R(0);
+        if (lxy != R(0)) {
+            const int z0 = o.loc.b[2] > 0 ? o.loc.b[2] : 0;
+            const int z1 = (o.loc.b[2] + o.loc.c[2]) < o.n[2] ? (o.loc.b[2] + o.loc.c[2]) : o.n[2];
+            for (int z = z0 + lane; z < z1; z += 32) {
+                const R w = simpson_w<R>(z, o.loc.b[2], o.loc.c[2]) * p2(z);
+                const R rz = R(o.dx[2]) * R(z - o.n[2] / 2);
+                s0 += w;
+                sz += w * rz;
+                szz += w * rz * rz;
+            }
+        }
+        const R rx = R(o.dx[0]) * R(x - o.n[0] / 2), ry = R(o.dx[1]) * R(y - o.n[1] / 2);
+        const R ls0 = lxy * s0;
+        const R q7[kLocQ] = {ls0, rx * ls0, ry * ls0, lxy * sz, rx * rx * ls0, ry * ry * ls0, lxy * szz};
+#pragma unroll
+        for (int q = 0; q < kLocQ; ++q) warp_sum_to<R>(q7[q], scratch, o.nbox + q);
+    }
+    __syncthreads();
+    block_partials(scratch, o.nq, o.partials);
 }
 template <typename R>
 cudaError_t launch_observe_real(const Cx<R>* psi, const ObsArgs& o, cudaStream_t s, int* grid_out) {
