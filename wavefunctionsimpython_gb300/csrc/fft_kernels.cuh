@@ -163,7 +163,10 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_strided_ker
 // the elements it later reads (rows t + P*i of its column), so the staging
 // buffers need no block barrier: cp.async.wait_group orders a thread's own
 // copies before its reads.
-// Shared memory: the transpose buffer plus two staging tiles (3 L W elements).
+// Shared memory: two staging tiles (2 L W elements). A tile, once loaded into
+// registers, is the transpose buffer of its own item: in the first transpose
+// thread t writes rows k2*P + t, which are rows it staged itself (rows = t mod P),
+// and the inverse transpose follows a block barrier.
 // ---------------------------------------------------------------------------
 template <int BYTES>
 __device__ __forceinline__ void cp_async_elem(void* smem, const void* gmem) {
@@ -179,12 +182,11 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 template <typename R, int P, int Q, int W, int OP>
-__global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS)
+__global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PIPE)
     fft_strided_pipe_kernel(const PassArgs<R> a, int64_t nitems) {
     constexpr int L = P * Q;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Cx<R>* sm = reinterpret_cast<Cx<R>*>(smem_raw);
-    Cx<R>* stage = sm + L * W;  // [2][L][W]
+    Cx<R>* stage = reinterpret_cast<Cx<R>*>(smem_raw);  // [2][L][W]
     const int tid = threadIdx.x, c = tid % W, t = tid / W;
     const int rs = int(a.row_stride);
     auto issue = [&](int64_t item, int slot) {
@@ -214,7 +216,8 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS)
         const int col = tile * W + c;
         const bool active = col < a.ncols;
         Cx<R>* base = a.data + outer * a.outer_stride + col;
-        const Cx<R>* src = stage + slot * (L * W) + c;
+        Cx<R>* sm = stage + slot * (L * W);  // this item's staging tile, reused as its transpose buffer
+        const Cx<R>* src = sm + c;
         Cx<R> a1[Q], a2[P];
         if (t < P) {
 #pragma unroll
@@ -242,7 +245,7 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS)
                 for (int i = 0; i < Q; ++i) base[(t + P * i) * rs] = a1[i];
             }
         }
-        __syncthreads();  // the next item's stage 1 rewrites the transpose buffer
+        __syncthreads();  // this tile is restaged for the item after next
         slot ^= 1;
     }
     cp_async_wait<0>();
@@ -364,7 +367,7 @@ struct ContigW {
     static constexpr int value = (256 / T) > 0 ? (256 / T) : 1;
 };
 
-// The pipelined strided pass is used where its three L x W tiles leave room for two
+// The pipelined strided pass is used where its two L x W tiles leave room for two
 // CTAs per SM; WFS_STRIDED_PIPELINE=0 in the environment selects the plain kernel
 // (for A/B timing).
 inline bool strided_pipeline_enabled() {
@@ -388,7 +391,7 @@ template <typename R, int L, int OP>
 cudaError_t run_strided_pipe(const PassArgs<R>& a, int64_t outer_count, cudaStream_t s) {
     constexpr int P = PlanOf<L>::P, Q = PlanOf<L>::Q, T = cmax(P, Q);
     constexpr int W = StridedW<R, T>::value;
-    const size_t smem = 3 * size_t(L) * W * sizeof(Cx<R>);
+    const size_t smem = 2 * size_t(L) * W * sizeof(Cx<R>);
     auto kern = fft_strided_pipe_kernel<R, P, Q, W, OP>;
     static int blocks_per_sm = 0;
     if (blocks_per_sm == 0) {
@@ -412,7 +415,7 @@ cudaError_t run_strided(const PassArgs<R>& a0, int64_t outer_count, cudaStream_t
     constexpr int W = StridedW<R, T>::value;
     PassArgs<R> a = a0;
     a.tiles = (a.ncols + W - 1) / W;
-    if constexpr (3 * size_t(L) * W * sizeof(Cx<R>) <= 112 * 1024) {
+    if constexpr (2 * size_t(L) * W * sizeof(Cx<R>) <= 112 * 1024) {
         if (strided_pipeline_enabled() && outer_count * a.tiles > int64_t(2) * device_sm_count())
             return run_strided_pipe<R, L, OP>(a, outer_count, s);
     }

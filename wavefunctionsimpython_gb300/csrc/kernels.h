@@ -14,6 +14,9 @@
 #ifndef WFS_MINB_PASS
 #define WFS_MINB_PASS 2
 #endif
+#ifndef WFS_MINB_PIPE
+#define WFS_MINB_PIPE 2
+#endif
 #ifndef WFS_MINB_PLANE
 #define WFS_MINB_PLANE 3
 #endif
