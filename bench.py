@@ -541,7 +541,7 @@ def run_surrogate(args):
         lib.wfs_fno_make_input(F._ptr(psi), F._ptr(gen.V), float(cfg.vscale), F._ptr(a2), F._ptr(x), G, cfg.n3, sp)
         lib.wfs_fno_scale_samples(F._ptr(prior), F._ptr(a2), 1, G, cfg.n3, sp)
         for k in range(0, G, IB):
-            model.forward(x[k:k + IB], prior[k:k + IB], IB, out=out[k:k + IB])
+            model.forward(x[k:k + IB], prior[k:k + IB], IB, out=out[k:k + IB], keep_pre=False)
         lib.wfs_fno_scale_samples(F._ptr(out), F._ptr(a2), 0, G, cfg.n3, sp)
         lib.wfs_fno_sample_norms(F._ptr(out), None, cfg.n3, G, F._ptr(a2), None, sp)
 

@@ -145,6 +145,28 @@ def test_forward_and_backward_match_oracle(torch):
         assert rel(g[name], ref_g) < 5e-3, name
 
 
+def test_inference_forward_without_pre_activations_is_identical(torch):
+    """forward(keep_pre=False) skips the pre-activation stores that only backward() reads;
+    the prediction must be bit-identical to the training-mode forward."""
+    from wavefunctionsimpython_gb300.fno import FNO, FnoConfig
+
+    N, m, Cw, L, H, B = 16, 4, 8, 3, 16, 2
+    cfg = FnoConfig(N=N, width=Cw, modes=m, layers=L, hidden=H)
+    p = fo.init_params(Cw, m, L, H, seed=11, zero_last=False)
+    rng = np.random.default_rng(11)
+    x = rng.normal(size=(B, 4, N, N, N)).astype(np.float32).astype(np.float64)
+    prior = rng.normal(size=(B, 2, N, N, N)).astype(np.float32).astype(np.float64)
+    model = FNO(cfg, seed=0)
+    model.set_params(_oracle_to_model(p))
+    xt, pt = packed(torch, x), packed(torch, prior)[:, 0]
+    a = torch.empty((B, N ** 3), dtype=torch.complex64, device="cuda")
+    b = torch.empty_like(a)
+    model.forward(xt, pt, B, out=a)
+    model.forward(xt, pt, B, out=b, keep_pre=False)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+
+
 def test_adam_matches_formula(torch):
     lib = _lib()
     rng = np.random.default_rng(2)
