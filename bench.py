@@ -431,7 +431,9 @@ def run_batch(args):
             "clocks": clk.summary(), "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": "batch_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "alg_bytes_per_launch": 24 * sites,
-                         "traffic": None},
+                         "traffic": ncu_traffic("batch"),
+                         "traffic_note": "DRAM bytes per launch from ncu: the largest instances' stage data "
+                                         "exceeds L2 and is re-read"},
             "transmitted_probability_mean": float(np.mean(probs))}
     print(json.dumps(line))
     return 0

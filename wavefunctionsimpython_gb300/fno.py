@@ -4,8 +4,8 @@ psi(t + K dt) ~ prior + FNO(psi(t), V), where prior is a coarse split step of th
 same interval (``prior_steps`` Strang steps of K dt / prior_steps, run by the
 batch engine) and the network (include/wfs_fno.h, csrc/fno.cu) learns the
 correction. The exact propagator (K plain split steps) is both the training
-target and the judge: a jump whose relative L2 error or norm error exceeds the
-tolerance is rejected and re-run with the plain method.
+target and the acceptance test: a jump whose relative L2 error or norm error
+exceeds the tolerance is rejected and re-run with the plain method.
 
 The reference has no learned propagator; the surrogate's trajectories come from
 the same split step as sources/sim_state.py:641-697 (this package's engine), its
