@@ -128,6 +128,21 @@ struct PassScope {
     }
 };
 
+// The device wait-status word (dflag[1]) is queued into pinned memory before a host sync and
+// read after it, so checking it adds no synchronisation.
+cudaError_t queue_status(wfs_handle* h) {
+    return cudaMemcpyAsync(h->hres + 255, h->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+}
+// After the sync that followed queue_status: WFS_ERR_TIMEOUT when a bounded device-side wait
+// gave up since the last check (the word is then cleared).
+int take_status(wfs_handle* h) {
+    int* s = reinterpret_cast<int*>(h->hres + 255);
+    if (*s == 0) return WFS_OK;
+    *s = 0;
+    cudaMemsetAsync(h->dflag + 1, 0, sizeof(int), h->stream);
+    return set_err(h, WFS_ERR_TIMEOUT, "a bounded device-side wait of a copy-staged pass gave up");
+}
+
 int ensure_partials(wfs_handle* h, size_t need) {
     if (need <= h->partials_cap) return WFS_OK;
     if (h->partials) cudaFree(h->partials);
@@ -192,6 +207,7 @@ PassArgs<R> base_args(wfs_handle* h, int axis) {
     a.data = reinterpret_cast<Cx<R>*>(h->psi);
     a.tw = reinterpret_cast<const Cx<R>*>(h->tw[axis]);
     a.scale = R(1);
+    a.status = h->dflag + 1;
     return a;
 }
 
@@ -440,7 +456,9 @@ int do_observe(wfs_handle* h, const wfs_box* boxes, int nbox, const wfs_box* loc
     if ((rc = observe_launch<R>(h, o, h->dres))) return rc;
     if (o.nq) {
         CK(cudaMemcpyAsync(h->hres, h->dres, o.nq * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(queue_status(h));
         CK(cudaStreamSynchronize(h->stream));
+        if ((rc = take_status(h))) return rc;
     }
     finish_obs(h, o, h->hres, prob, r, r2);
     return WFS_OK;
@@ -471,8 +489,10 @@ int do_run_split(wfs_handle* h, int nsteps, double dt, double mass, int interval
     if (rc == WFS_OK && nrec) {
         std::vector<double> raw(size_t(nrec) * o.nq);
         cudaError_t e = cudaMemcpyAsync(raw.data(), dser, raw.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = queue_status(h);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess) rc = set_err(h, WFS_ERR_CUDA, std::string("series copy: ") + cudaGetErrorString(e));
+        if (rc == WFS_OK) rc = take_status(h);
         for (int k = 0; k < nrec && rc == WFS_OK; ++k) {
             double rr[3], rr2[3];
             finish_obs(h, o, raw.data() + size_t(k) * o.nq, prob_series ? prob_series + size_t(k) * nbox : nullptr, rr, rr2);
@@ -599,7 +619,9 @@ int wfs_create(const wfs_grid_desc* d, wfs_handle** out) {
     if (e == cudaSuccess) e = cudaMalloc(&h->V, h->count * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&h->dres, 256 * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost(&h->hres, 256 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&h->dflag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&h->dflag, 2 * sizeof(int));  // [0] non-finite, [1] wait status
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->dflag, 0, 2 * sizeof(int), h->stream);
+    if (e == cudaSuccess) std::memset(h->hres, 0, 256 * sizeof(double));
     if (e == cudaSuccess) e = cudaMemsetAsync(h->psi, 0, h->count * h->elem, h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->V, 0, h->count * sizeof(float2), h->stream);
     if (e != cudaSuccess) return fail(set_err(h, WFS_ERR_CUDA, std::string("allocation: ") + cudaGetErrorString(e)));
@@ -632,8 +654,9 @@ const char* wfs_last_error(const wfs_handle* h) { return h ? h->err.c_str() : g_
 
 int wfs_synchronize(wfs_handle* h) {
     if (!h) return dispatch_err(h);
+    CK(queue_status(h));
     CK(cudaStreamSynchronize(h->stream));
-    return WFS_OK;
+    return take_status(h);
 }
 
 int wfs_potential_clear(wfs_handle* h) {
@@ -834,8 +857,9 @@ int wfs_get_psi(wfs_handle* h, void* psi, int32_t to_device) {
     int rc = is_dbl(h) ? to_real<double>(h) : to_real<float>(h);
     if (rc) return rc;
     CK(cudaMemcpyAsync(psi, h->psi, h->count * h->elem, to_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+    CK(queue_status(h));
     CK(cudaStreamSynchronize(h->stream));
-    return WFS_OK;
+    return take_status(h);
 }
 
 int wfs_psi_device_ptr(wfs_handle* h, void** ptr) {

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdlib>
 
+#include "bulk_copy.cuh"
 #include "kernels.h"
 
 namespace wfs {
@@ -249,6 +250,104 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PIPE)
         slot ^= 1;
     }
     cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// Copy-engine staged strided pass (complex64): the pipelined pass with each
+// item's L x W tile brought into shared memory by one 3D tensor copy (x = column,
+// y = pencil row, z = outer slab) instead of Q cp.async copies per thread. Thread
+// 0 arms the slot's mbarrier and issues the copy of item k + gridDim.x while the
+// block transforms item k; the other threads issue no copies and compute no
+// addresses for them. Columns past ncols arrive zero-filled and are not stored.
+// Item k of a CTA lives in slot k & 1 and completes phase (k >> 1) & 1 of that
+// slot's barrier. A wait that gives up sets bit 0 of *status; thread 0 then
+// issues no further copies and, before the CTA exits, waits (bounded) for any
+// copy still in flight.
+// ---------------------------------------------------------------------------
+struct StridedStagedArgs {
+    PassArgs<float> p;
+    TensorMapImage map;  // psi as (ncols, L, outer) complex64 elements, box (W, L, 1)
+};
+
+template <int P, int Q, int W, int OP>
+__global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_STAGED)
+    fft_strided_staged_kernel(const __grid_constant__ StridedStagedArgs sa, int64_t nitems) {
+    using R = float;
+    constexpr int L = P * Q;
+    const PassArgs<R>& a = sa.p;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Cx<R>* stage = reinterpret_cast<Cx<R>*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));  // [2][L][W]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(stage + 2 * L * W);
+    const int tid = threadIdx.x, c = tid % W, t = tid / W;
+    const int rs = int(a.row_stride);
+    if (tid == 0) {
+        mbar_init(smem_addr(&bars[0]), 1);
+        mbar_init(smem_addr(&bars[1]), 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    bool expired = false;
+    auto issue = [&](int64_t item, int slot) {  // thread 0 only
+        if (expired) return;
+        const uint32_t bar = smem_addr(&bars[slot]);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, uint32_t(L * W * sizeof(Cx<R>)));
+        tensor_load_3d(smem_addr(stage + slot * (L * W)), &sa.map, int(item % a.tiles) * W, 0, int(item / a.tiles), bar);
+    };
+    auto sidx_f = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
+    auto sidx_i = [&](int k2, int n1) { return (k2 * Q + n1) * W + c; };
+    int64_t item = blockIdx.x;
+    if (tid == 0 && item < nitems) issue(item, 0);
+    int k = 0;
+    for (; item < nitems; item += gridDim.x, ++k) {
+        const int slot = k & 1;
+        const int64_t next = item + gridDim.x;
+        if (tid == 0 && next < nitems) issue(next, slot ^ 1);
+        if (!mbar_wait_bounded(smem_addr(&bars[slot]), uint32_t((k >> 1) & 1))) {
+            if (!expired && a.status) atomicOr(a.status, 1);
+            expired = true;
+        }
+        const int tile = int(item % a.tiles);
+        const int64_t outer = item / a.tiles;
+        const int col = tile * W + c;
+        const bool active = col < a.ncols;
+        Cx<R>* base = a.data + outer * a.outer_stride + col;
+        Cx<R>* sm = stage + slot * (L * W);  // this item's staging tile, reused as its transpose buffer
+        const Cx<R>* src = sm + c;
+        Cx<R> a1[Q], a2[P];
+        if (t < P) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) a1[i] = src[(t + P * i) * W];
+        }
+        if constexpr (OP == OP_PLAIN) {
+            if (a.dir < 0) two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
+            else two_stage<P, Q, +1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
+            if (active && t < Q) {
+#pragma unroll
+                for (int kk = 0; kk < P; ++kk) base[(t + Q * kk) * rs] = scale(a2[kk], a.scale);
+            }
+        } else {  // OP_KIN
+            two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
+            if (t < Q) {
+                Cx<R> cf = mk<R>(R(0), R(0));
+                if (active) cf = scale(cmul(a.k_c1[col / a.c2n], a.k_c2[col % a.c2n]), a.scale);
+#pragma unroll
+                for (int kk = 0; kk < P; ++kk) a2[kk] = cmul(a2[kk], cmul(a.k_row[t + Q * kk], cf));
+            }
+            __syncthreads();
+            two_stage<Q, P, +1, TW_ROW>(a2, a1, sm, tw_rows<Q, P, P, Q>(a.tw), t, sidx_i);
+            if (active && t < P) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) base[(t + P * i) * rs] = a1[i];
+            }
+        }
+        __syncthreads();  // this slot is refilled with the item after next
+    }
+    // after an expired wait a copy may still be landing: wait (bounded) before the CTA exits
+    if (tid == 0 && expired) {
+        if (k > 0) mbar_wait_bounded(smem_addr(&bars[(k - 1) & 1]), uint32_t(((k - 1) >> 1) & 1));
+        if (k > 1) mbar_wait_bounded(smem_addr(&bars[(k - 2) & 1]), uint32_t(((k - 2) >> 1) & 1));
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -20,6 +20,11 @@
 #ifndef WFS_MINB_PLANE
 #define WFS_MINB_PLANE 3
 #endif
+// The copy-staged strided pass computes no per-thread copy addresses and fits 80
+// registers without spilling, so it is budgeted for 3 resident blocks per SM.
+#ifndef WFS_MINB_STAGED
+#define WFS_MINB_STAGED 3
+#endif
 
 namespace wfs {
 
@@ -85,6 +90,7 @@ struct PassArgs {
     const Cx<R>* ephase;
     // OP_OBS (contiguous, read-only): observe scale * F^-1(x); rows are (x, y) = (q / ny, q % ny)
     ObsArgs obs;
+    int* status;            // copy-staged passes: bit 0 set when a bounded wait gave up (may be null)
 };
 
 template <typename R>
