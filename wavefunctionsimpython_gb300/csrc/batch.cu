@@ -158,10 +158,16 @@ __device__ __forceinline__ void run_prog(const InstDesc& in, int prog, int rank,
 }
 
 constexpr int kBatchThreads = 256;
+// resident blocks per SM the batch kernel is register-budgeted for (build-time tuning knob);
+// measured on the 256-instance sweep: 0.580 ms per step at 2, 0.611 ms at 3 (small spills,
+// and more instances in flight overflow L2 further)
+#ifndef WFS_MINB_BATCH
+#define WFS_MINB_BATCH 2
+#endif
 constexpr size_t kBatchSmem = 24 * 1024;
 
 template <bool SWAP>
-__global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(const InstDesc* __restrict__ insts,
+__global__ void __launch_bounds__(kBatchThreads, WFS_MINB_BATCH) batch_kernel(const InstDesc* __restrict__ insts,
                                                               const int* __restrict__ order, int prog) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Cx<float>* sm = reinterpret_cast<Cx<float>*>(smem_raw);
