@@ -102,8 +102,10 @@ def scenario(n, L, dbl, absorber=True):
 @pytest.mark.parametrize("schedule", ["auto", "axis"])
 @pytest.mark.parametrize("dbl", [False, True])
 @pytest.mark.parametrize("n", [(32, 32, 32), (64, 64, 64), (16, 48, 32), (48, 48, 48), (96, 32, 64), (8, 128, 16),
-                               (16, 96, 96), (8, 128, 128), (4, 256, 256)])
+                               (16, 96, 96), (8, 128, 128), (4, 256, 256), (384, 64, 6)])
 def test_split_step(Engine, n, dbl, schedule):
+    # (384, 64, 6): the y passes have 384 tiles of 32 columns with 6 in the grid, so the
+    # copy-staged strided pass runs with zero-filled columns past the edge
     L = tuple(0.4 * x for x in n)
     dx, V, psi0 = scenario(n, L, dbl)
     e = Engine(n, L, double_precision=dbl)
