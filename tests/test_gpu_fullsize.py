@@ -88,16 +88,55 @@ def test_double_slit_256_two_steps_match_fp64_oracle(slit):
 
 
 def test_double_slit_256_unitarity_and_time_reversal(slit):
-    """Without the absorber V is real: the step is unitary and dt -> -dt undoes it."""
+    """Without the absorber V is real: the step is unitary and dt -> -dt undoes it
+    (measured: norm +1.4e-5 over 200 steps, reversal 2.8e-5)."""
     V = np.zeros(slit.n, np.complex64)
     orc.add_potential_wall(V, slit.dx, slit.walls[0])
     e = engine_for(slit, V)
     psi0 = e.get_psi()
     n0 = e.norm()
     e.step_split(200, slit.dt, 1.0)
-    assert abs(e.norm() / n0 - 1.0) < 1e-4
+    assert abs(e.norm() / n0 - 1.0) < 5e-5
     e.step_split(200, -slit.dt, 1.0)
-    assert rel(e.get_psi(), psi0) < 2e-4
+    assert rel(e.get_psi(), psi0) < 1e-4
+
+
+def test_double_slit_256_2000_step_trajectory_vs_complex128(slit):
+    """The whole double-slit run of the benchmark (2000 steps, absorber on, P(x > 1) every
+    20 steps) in complex64 against the same run in complex128, whose single steps match
+    the FP64 oracle to 1e-11. An FFT-based oracle run of 2000 steps at 256^3 would take
+    hours on the host, so the complex128 engine stands in for it here.
+
+    Rounded butterfly constants shrink every complex64 transform by a fixed fraction
+    (-3.2e-7 of the norm per step at 256^3, -5.6e-4 over this run). The engine folds the
+    inverse of that gain into its kinetic tables, which leaves 9.6e-5 relative L2 on psi
+    and 2.4e-5 on the P(x > 1) series after 2000 steps. The bounds below sit at about
+    twice the measured values and below what the run gives without the compensation
+    (2.9e-4 on psi, 1.9e-4 on the series)."""
+    from wavefunctionsimpython_gb300 import Engine
+
+    dx = 80.0 / 256
+    inner = 40.0 - 16 * dx
+    b = np.array([1.0, -inner, -inner])
+    t = np.array([inner, inner, inner])
+    bv = ((b + 40.0) / dx).astype(np.int64)
+    tv = ((t + 40.0) / dx).astype(np.int64) + 1
+    cnt = np.minimum(tv - bv, 256 - bv)
+    cnt = np.where(cnt % 2 == 0, cnt - 1, cnt)  # Simpson needs an odd sample count
+    box = (tuple(int(v) for v in bv), tuple(int(v) for v in cnt))
+    runs = {}
+    for dbl in (False, True):
+        e = Engine(slit.n, slit.extent, double_precision=dbl)
+        e.set_potential(slit.potential())
+        e.init_gaussian(slit.sigma, slit.r0, slit.k0)
+        probs, _ = e.run_split(2000, slit.dt, 1.0, 20, [box], None)
+        runs[dbl] = (np.asarray(probs, np.float64).ravel(), e.get_psi().astype(np.complex128), e.norm())
+        e.close()
+    (p64, psi64, n64), (p128, psi128, n128) = runs[False], runs[True]
+    assert p128.size == 100 and p128.max() > 0.3  # a third of the packet has passed the slits
+    assert rel(psi64, psi128) < 2e-4
+    assert np.max(np.abs(p64 - p128)) < 6e-5
+    assert abs(n64 / n128 - 1.0) < 2e-4
 
 
 def test_double_slit_256_linearity(slit):
@@ -119,10 +158,12 @@ def test_double_slit_256_linearity(slit):
 
 
 def test_batched_sweep_full_mix():
-    """The 256-instance sweep (128x32^3, 64x48^3, 48x64^3, 16x96^3) for 500 steps: two
-    instances of every size agree with the single-grid engine, and every instance keeps
-    its norm (barriers only, no absorber), both to 5e-4: 500 complex64 steps accumulate
-    FP32 rounding beyond the 1e-5 bar that short runs meet against the FP64 oracle."""
+    """The 256-instance sweep (128x32^3, 64x48^3, 48x64^3, 16x96^3) for 500 steps. Every
+    instance keeps its norm (barriers only, no absorber) to 2e-4 (measured at most 8.7e-5),
+    and two instances of every size agree with the single-grid engine to 2e-5 (measured
+    6.5e-6) and with the complex128 engine to 1e-4 (measured 3.8e-5). Over 500 steps
+    complex64 rounding accumulates past the 1e-5 that short runs meet against the FP64
+    oracle."""
     from wavefunctionsimpython_gb300 import Engine
     from wavefunctionsimpython_gb300._lib import Batch
 
@@ -143,19 +184,24 @@ def test_batched_sweep_full_mix():
     b.synchronize()
     for i in range(len(sizes)):
         n1 = float(np.sum(np.abs(b.get_psi(i).astype(np.complex128)) ** 2))
-        assert abs(n1 / norms0[i] - 1.0) < 5e-4, i
+        assert abs(n1 / norms0[i] - 1.0) < 2e-4, i
     first = {}
     for i, n in enumerate(sizes):
         first.setdefault(n, []).append(i)
     for n, idx in first.items():
         for i in (idx[0], idx[-1]):
             U, w, k0, sig, x0 = params[i]
-            e = Engine((n,) * 3, (L,) * 3)
-            e.add_wall(U, (0, 0, 0), (1, 0, 0), w)
-            e.init_gaussian((sig,) * 3, (x0, 0, 0), (k0, 0, 0))
-            e.step_split(500, 0.01, 1.0)
-            assert rel(b.get_psi(i), e.get_psi()) < 5e-4, (n, i)
-            e.close()
+            single = {}
+            for dbl in (False, True):
+                e = Engine((n,) * 3, (L,) * 3, double_precision=dbl)
+                e.add_wall(U, (0, 0, 0), (1, 0, 0), w)
+                e.init_gaussian((sig,) * 3, (x0, 0, 0), (k0, 0, 0))
+                e.step_split(500, 0.01, 1.0)
+                single[dbl] = e.get_psi()
+                e.close()
+            psi_b = b.get_psi(i)
+            assert rel(psi_b, single[False]) < 2e-5, (n, i)
+            assert rel(psi_b, single[True]) < 1e-4, (n, i)
 
 
 @pytest.mark.parametrize("n", [512, 1024])

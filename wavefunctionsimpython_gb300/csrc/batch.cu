@@ -32,6 +32,7 @@ struct InstDesc {
     const Cx<float>* kin;   // [half x][half y][half z][full x][full y][full z], L each
     const Cx<float>* tw;    // two-stage twiddle table (3L entries, two_stage_roots)
     int L;
+    float sy;               // 1/sqrt(L) rounded from double on the host (y stages, unpaired z stages)
 };
 
 enum Prog { PROG_ENTER = 0, PROG_STEP_HALF = 1, PROG_STEP_FULL = 2, PROG_FINISH = 3 };
@@ -97,7 +98,7 @@ __device__ __forceinline__ void z_plain_tile(const InstDesc& in, int tile, Cx<fl
     auto sf = [&](int k2, int n1) { return r * RS + k2 * (P + 1) + n1; };
     const int tt = in_block ? t : T;
     two_stage<P, Q, SIGN, TW_ANGLE>(a1, a2, sm, in.tw, tt, sf);
-    const float sc = rsqrtf(float(L));
+    const float sc = in.sy;
     if (active && t < Q) {
 #pragma unroll
         for (int k = 0; k < P; ++k) st_l2<float>(rp + t + Q * k, scale(a2[k], sc));
@@ -116,7 +117,7 @@ __device__ __forceinline__ void run_prog(const InstDesc& in, int prog, int rank,
     const int ntile_yp = (L + B::WS - 1) / B::WS;          // y tiles per plane
     const int ntile_y = ntile_yp * L;
     const int ntile_z = int((plane + B::WC - 1) / B::WC);   // z rows of the instance
-    const float sy = rsqrtf(float(L));
+    const float sy = in.sy;
     auto y_stage = [&](auto SIGNc) {
         constexpr int SIGN = decltype(SIGNc)::value;
         for (int tile = rank; tile < ntile_y; tile += CL) {
@@ -276,8 +277,15 @@ int ensure_tables(wfs_batch* b, double dt, double mass) {
             const int L = b->L[i];
             const double dx = b->extent[i] / L;
             Cx<float>* p = h.data() + b->kin_off[i];
-            for (int a = 0; a < 3; ++a) kinetic_axis<float>(L, dx, dt, mass, 0.25, p + a * L);
-            for (int a = 0; a < 3; ++a) kinetic_axis<float>(L, dx, dt, mass, 0.5, p + (3 + a) * L);
+            // A run of S steps makes S + 1 x passes (S steps and the finishing half step) and
+            // S + 1 sets of y/z transforms (S steps, plus the entry and exit transforms), so
+            // each x factor carries the inverse gain of one x pass and one y/z set.
+            const int n3[3] = {L, L, L};
+            double gx = 1.0, gyz = 1.0;
+            split_step_gains<float>(n3, &gx, &gyz);
+            const double amp = 1.0 / std::sqrt(gx * gyz);
+            for (int a = 0; a < 3; ++a) kinetic_axis<float>(L, dx, dt, mass, 0.25, p + a * L, a == 0 ? amp : 1.0);
+            for (int a = 0; a < 3; ++a) kinetic_axis<float>(L, dx, dt, mass, 0.5, p + (3 + a) * L, a == 0 ? amp : 1.0);
         }
         BCK(cudaMemcpy(b->kin, h.data(), h.size() * sizeof(Cx<float>), cudaMemcpyHostToDevice));
         b->kin_dt = dt;
@@ -434,6 +442,7 @@ int wfs_batch_create(const wfs_batch_desc* d, wfs_batch** out) {
         hd[i].kin = b->kin + b->kin_off[i];
         hd[i].tw = b->tw + b->tw_off[b->L[i]];
         hd[i].L = b->L[i];
+        hd[i].sy = float(1.0 / std::sqrt(double(b->L[i])));
     }
     std::vector<int> ord(b->ninst);
     for (int i = 0; i < b->ninst; ++i) ord[i] = i;

@@ -34,7 +34,7 @@ thread_local std::string g_error;
 enum Rep { REP_REAL = 0, REP_G = 1, REP_H = 2, REP_PENDING = 3 };
 
 struct KinTables {
-    double dt = std::nan(""), mass = std::nan(""), frac = std::nan("");
+    double dt = std::nan(""), mass = std::nan(""), frac = std::nan(""), amp = std::nan("");
     void* k[3] = {nullptr, nullptr, nullptr};
 };
 
@@ -83,6 +83,10 @@ struct wfs_handle {
     int64_t prof_count[WFS_NPASS];
     int64_t launches;
     int schedule;         // WFS_SCHEDULE_*
+    // amplitude folded into the x factor of the stepping kinetic tables: the inverse of
+    // the transforms' mean gain from rounded constants (split_step_gains), one step's
+    // worth in the full table and half of the y/z part in the half table
+    double amp_full, amp_half;
 };
 
 namespace {
@@ -164,10 +168,12 @@ int upload_roots(wfs_handle* h, int axis) {
 }
 
 // Per-axis kinetic factors exp(-i k^2 dt frac / m), k = 2 pi fftfreq(N, dx)
-// (sources/sim_state.py:275-278, kinetic_operator.cu:20-23).
+// (sources/sim_state.py:275-278, kinetic_operator.cu:20-23). The x factor is scaled by
+// amp before rounding (1 for the kinetic operator itself; the engine's gain compensation
+// for the tables of the split step).
 template <typename R>
-int ensure_kin(wfs_handle* h, KinTables& kt, double dt, double mass, double frac) {
-    if (kt.dt == dt && kt.mass == mass && kt.frac == frac && kt.k[0]) return WFS_OK;
+int ensure_kin(wfs_handle* h, KinTables& kt, double dt, double mass, double frac, double amp = 1.0) {
+    if (kt.dt == dt && kt.mass == mass && kt.frac == frac && kt.amp == amp && kt.k[0]) return WFS_OK;
     // kernels already queued on the engine's stream may still read the old table
     if (kt.k[0]) CK(cudaStreamSynchronize(h->stream));
     for (int a = 0; a < 3; ++a) {
@@ -177,7 +183,8 @@ int ensure_kin(wfs_handle* h, KinTables& kt, double dt, double mass, double frac
             const int fi = (i < (L + 1) / 2) ? i : i - L;  // fftfreq ordering
             const double k = 2.0 * M_PI * double(fi) / (double(L) * h->dx[a]);
             const double ang = -k * k * dt * frac / mass;
-            v[i] = mk<R>(R(std::cos(ang)), R(std::sin(ang)));
+            const double m = (a == 0) ? amp : 1.0;
+            v[i] = mk<R>(R(m * std::cos(ang)), R(m * std::sin(ang)));
         }
         if (!kt.k[a]) CK(cudaMalloc(&kt.k[a], L * sizeof(Cx<R>)));
         CK(cudaMemcpy(kt.k[a], v.data(), L * sizeof(Cx<R>), cudaMemcpyHostToDevice));
@@ -185,6 +192,7 @@ int ensure_kin(wfs_handle* h, KinTables& kt, double dt, double mass, double frac
     kt.dt = dt;
     kt.mass = mass;
     kt.frac = frac;
+    kt.amp = amp;
     return WFS_OK;
 }
 
@@ -288,7 +296,7 @@ bool use_plane(const wfs_handle* h) {
 template <typename R>
 int finish_pending(wfs_handle* h) {
     if (h->rep != REP_PENDING) return WFS_OK;
-    int rc = ensure_kin<R>(h, h->kin_half, h->pend_dt, h->pend_mass, 0.25);
+    int rc = ensure_kin<R>(h, h->kin_half, h->pend_dt, h->pend_mass, 0.25, h->amp_half);
     if (rc) return rc;
     rc = pass_x_kin<R>(h, h->kin_half);
     if (rc) return rc;
@@ -349,8 +357,8 @@ int split_steps(wfs_handle* h, int nsteps, double dt, double mass) {
         if ((rc = finish_pending<R>(h))) return rc;
     }
     if ((rc = ensure_ephase<R>(h, dt))) return rc;
-    if ((rc = ensure_kin<R>(h, h->kin_half, dt, mass, 0.25))) return rc;
-    if ((rc = ensure_kin<R>(h, h->kin_full, dt, mass, 0.5))) return rc;
+    if ((rc = ensure_kin<R>(h, h->kin_half, dt, mass, 0.25, h->amp_half))) return rc;
+    if ((rc = ensure_kin<R>(h, h->kin_full, dt, mass, 0.5, h->amp_full))) return rc;
     bool merged = (h->rep == REP_PENDING);
     if (!merged && (rc = to_H<R>(h))) return rc;
     const bool plane = use_plane(h);
@@ -590,6 +598,7 @@ int wfs_create(const wfs_grid_desc* d, wfs_handle** out) {
     h->steps_done = 0;
     h->launches = 0;
     h->schedule = WFS_SCHEDULE_AUTO;
+    h->amp_full = h->amp_half = 1.0;
     for (int k = 0; k < WFS_NPASS; ++k) { h->prof_ms[k] = 0.0; h->prof_count[k] = 0; }
     h->dtype = d->dtype;
     h->device = d->device;
@@ -629,6 +638,17 @@ int wfs_create(const wfs_grid_desc* d, wfs_handle** out) {
     for (int a = 0; a < 3 && rc == WFS_OK; ++a)
         if (fft_length_supported(h->n[a], is_dbl(h))) rc = is_dbl(h) ? upload_roots<double>(h, a) : upload_roots<float>(h, a);
     if (rc) return fail(rc);
+    bool all_fft = true;
+    for (int a = 0; a < 3; ++a) all_fft = all_fft && fft_length_supported(h->n[a], is_dbl(h));
+    if (all_fft) {
+        // per x pass: its own two x transforms; per step: one set of y/z transforms, whose
+        // correction the full table carries whole and each of the two half tables by half
+        double gx = 1.0, gyz = 1.0;
+        if (is_dbl(h)) split_step_gains<double>(h->n, &gx, &gyz);
+        else split_step_gains<float>(h->n, &gx, &gyz);
+        h->amp_full = 1.0 / std::sqrt(gx * gyz);
+        h->amp_half = 1.0 / std::sqrt(gx * std::sqrt(gyz));
+    }
     *out = h;
     return WFS_OK;
 }

@@ -142,14 +142,14 @@ inline AbsorbDev absorbing_dev(const wfs_absorbing* a) {
     return ad;
 }
 
-// exp(-i k^2 dt frac / m) for k = 2 pi fftfreq(L, dx), in precision R.
+// amp * exp(-i k^2 dt frac / m) for k = 2 pi fftfreq(L, dx), rounded to precision R.
 template <typename R>
-inline void kinetic_axis(int L, double dx, double dt, double mass, double frac, Cx<R>* out) {
+inline void kinetic_axis(int L, double dx, double dt, double mass, double frac, Cx<R>* out, double amp = 1.0) {
     for (int i = 0; i < L; ++i) {
         const int fi = (i < (L + 1) / 2) ? i : i - L;
         const double k = 2.0 * M_PI * double(fi) / (double(L) * dx);
         const double ang = -k * k * dt * frac / mass;
-        out[i] = mk<R>(R(std::cos(ang)), R(std::sin(ang)));
+        out[i] = mk<R>(R(amp * std::cos(ang)), R(amp * std::sin(ang)));
     }
 }
 
@@ -171,6 +171,77 @@ inline bool two_stage_roots(int L, Cx<R>* out) {
     for (int t = 0; t < Q; ++t)
         for (int k = 0; k < P; ++k) out[2 * L + t * P + k] = root(t * k);
     return true;
+}
+
+// ---------------------------------------------------------------------------
+// Mean energy gain of the transforms as built from working-precision constants.
+//
+// The butterflies multiply by roots of unity rounded to R, and a rounded root is
+// not exactly of modulus 1: in complex64, cos(pi/8), sin(pi/8) and sqrt(1/2) all
+// round to a slightly shorter root (|w|^2 - 1 = -5.7e-8 and -3.4e-8). Every
+// element meets these same constants in every transform, so the norm of a
+// complex64 run drifts by a fixed fraction per step (about -3.2e-7 per step at
+// 256^3) instead of random-walking. These functions compute the mean gain
+// trace(M^H M) / N^2 of each transform from the very constants the kernels use
+// (compile-time roots of common.cuh, the uploaded twiddle tables, the rounded
+// scale factors), assuming uncorrelated data between stages; the engine folds
+// the inverse into its kinetic tables.
+// ---------------------------------------------------------------------------
+template <typename R>
+inline double rounded_norm2(double c, double s) {
+    const double cr = double(R(c)), sr = double(R(s));
+    return cr * cr + sr * sr;
+}
+// |w|^2 of exp(2 pi i m / n) as twiddle_const applies it (multiples of n/4 are exact).
+template <typename R>
+inline double const_root_norm2(long m, long n) {
+    m %= n;
+    if (m < 0) m += n;
+    if (m == 0 || 4 * m == n || 2 * m == n || 4 * m == 3 * n) return 1.0;
+    const Root w = root_of(m, n);
+    return rounded_norm2<R>(w.c, w.s);
+}
+// Mean energy gain of dft<N> (unnormalised DFT divided by N), following its
+// F x M decomposition in common.cuh.
+template <typename R>
+inline double dft_gain(int N) {
+    if (N <= 2 || N == 4) return 1.0;
+    if (N == 3) {
+        const double s3 = double(R(0.86602540378443864676372317075293618));
+        return (6.0 + 4.0 * s3 * s3) / 9.0;
+    }
+    const int F = (N % 4 == 0) ? 4 : ((N % 2 == 0) ? 2 : 3);
+    const int M = N / F;
+    double tw = 0.0;
+    for (int j = 0; j < F; ++j)
+        for (int k = 0; k < M; ++k) tw += const_root_norm2<R>(long(j) * k, N);
+    return dft_gain<R>(M) * (tw / double(F * M)) * dft_gain<R>(F);
+}
+// Mean energy gain of one two-stage transform of length L, without its scale factor.
+template <typename R>
+inline double fft_gain(int L) {
+    int P = 0, Q = 0;
+    if (!plan_pq(L, P, Q)) return 1.0;
+    double tw = 0.0;
+    for (int t = 0; t < P; ++t)
+        for (int k = 0; k < Q; ++k) {
+            const double a = -2.0 * 3.14159265358979323846 * double((t * k) % L) / double(L);
+            tw += rounded_norm2<R>(std::cos(a), std::sin(a));
+        }
+    return dft_gain<R>(Q) * (tw / double(P * Q)) * dft_gain<R>(P);
+}
+// Energy gain of one split step's transforms: the x pass (two x transforms, scale 1/nx
+// once) and the y/z work (two y transforms scaled by 1/sqrt(ny) each, two z transforms
+// scaled by 1/nz once), identical in the fused plane pass and the per-axis passes.
+template <typename R>
+inline void split_step_gains(const int n[3], double* g_x, double* g_yz) {
+    const double sx = double(R(1.0 / double(n[0])));
+    const double sy = double(R(1.0 / std::sqrt(double(n[1]))));
+    const double sz = double(R(1.0 / double(n[2])));
+    const double gx = fft_gain<R>(n[0]), gy = fft_gain<R>(n[1]), gz = fft_gain<R>(n[2]);
+    *g_x = gx * gx * (n[0] * sx) * (n[0] * sx);
+    const double gys = gy * n[1] * sy * sy;
+    *g_yz = gys * gys * gz * gz * (n[2] * sz) * (n[2] * sz);
 }
 
 }  // namespace wfs
