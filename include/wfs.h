@@ -92,6 +92,9 @@ const char* wfs_global_error(void);
 int wfs_create(const wfs_grid_desc* desc, wfs_handle** out);
 int wfs_destroy(wfs_handle* h);
 const char* wfs_last_error(const wfs_handle* h);
+/* Waits for the handle's stream. Propagation calls are asynchronous; a copy-staged
+ * pass whose bounded wait for a tile copy gave up is reported here, by wfs_get_psi
+ * and by the observation calls as WFS_ERR_TIMEOUT (the status is then cleared). */
 int wfs_synchronize(wfs_handle* h);
 
 /* Potential construction (sources/sim_state.py:210-255). */
