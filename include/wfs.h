@@ -180,6 +180,13 @@ enum wfs_schedule { WFS_SCHEDULE_AUTO = 0, WFS_SCHEDULE_AXIS = 1, WFS_SCHEDULE_P
 int wfs_set_schedule(wfs_handle* h, int32_t schedule);
 /* Number of kernels the engine has launched since creation. */
 int wfs_launch_count(wfs_handle* h, int64_t* out);
+/* Mean energy gain of one split step's transforms on an n[0] x n[1] x n[2] grid of dtype
+ * (WFS_C64 or WFS_C128), as built from rounded constants: *g_x for the x pass (two x
+ * transforms), *g_yz for the y/z work (two y and two z transforms). The engine divides
+ * its kinetic x factors by their square roots (one x pass and one y/z set per step).
+ * No counterpart in the reference: it reports the compensation of complex64 rounding
+ * that keeps long runs on the complex128 trajectory. Host-only; needs no GPU. */
+int wfs_split_step_gain(const int32_t n[3], int32_t dtype, double* g_x, double* g_yz);
 
 /* ------------------------------------------------------------------------
  * Batched sweep: many independent packets on uneven cubic grids advanced

@@ -33,7 +33,7 @@ EXPORTED = [
     "wfs_set_potential", "wfs_get_potential", "wfs_init_gaussian", "wfs_set_psi", "wfs_get_psi",
     "wfs_psi_device_ptr", "wfs_step_split", "wfs_step_taylor", "wfs_kinetic_operator", "wfs_potential_operator",
     "wfs_observe", "wfs_run_split", "wfs_norm", "wfs_profile_enable", "wfs_profile_read", "wfs_launch_count",
-    "wfs_set_schedule",
+    "wfs_set_schedule", "wfs_split_step_gain",
     "wfs_batch_create", "wfs_batch_destroy", "wfs_batch_last_error", "wfs_batch_synchronize",
     "wfs_batch_init_gaussian", "wfs_batch_add_wall", "wfs_batch_add_absorbing", "wfs_batch_set_potential",
     "wfs_batch_set_psi", "wfs_batch_get_psi", "wfs_batch_run", "wfs_batch_observe", "wfs_batch_set_config",
@@ -148,6 +148,7 @@ def load(path: str | os.PathLike | None = None):
         "wfs_profile_read": ([vp, dp, C.POINTER(C.c_int64), i32], C.c_int),
         "wfs_launch_count": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "wfs_set_schedule": ([vp, i32], C.c_int),
+        "wfs_split_step_gain": ([C.POINTER(C.c_int32), i32, dp, dp], C.c_int),
         "wfs_batch_create": ([C.POINTER(BatchDesc), C.POINTER(vp)], C.c_int),
         "wfs_batch_destroy": ([vp], C.c_int),
         "wfs_batch_last_error": ([vp], C.c_char_p),

@@ -1011,6 +1011,20 @@ int wfs_launch_count(wfs_handle* h, int64_t* out) {
     return WFS_OK;
 }
 
+int wfs_split_step_gain(const int32_t n[3], int32_t dtype, double* g_x, double* g_yz) {
+    if (!n || !g_x || !g_yz) return set_err(nullptr, WFS_ERR_ARG, "null argument");
+    if (dtype != WFS_C64 && dtype != WFS_C128) return set_err(nullptr, WFS_ERR_ARG, "dtype must be WFS_C64 or WFS_C128");
+    int nn[3];
+    for (int a = 0; a < 3; ++a) {
+        if (!fft_length_supported(n[a], dtype == WFS_C128))
+            return set_err(nullptr, WFS_ERR_UNSUPPORTED, "axis length not supported by the split step");
+        nn[a] = n[a];
+    }
+    if (dtype == WFS_C128) split_step_gains<double>(nn, g_x, g_yz);
+    else split_step_gains<float>(nn, g_x, g_yz);
+    return WFS_OK;
+}
+
 int wfs_plane_current(wfs_handle* h, const double center[3], const double normal[3], const double size[2],
                       const int32_t count[2], double mass, double* flux_out, void* density_out, int32_t to_device) {
     if (!h) return dispatch_err(h);
