@@ -65,7 +65,9 @@ cudaError_t run_strided_staged(const PassArgs<float>& a0, int64_t outer_count, c
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return cudaSuccess;
         std::memcpy(&sa.map, &map, sizeof(map));
-        const size_t smem = 128 + 2 * size_t(L) * W * sizeof(Cx<float>) + 2 * sizeof(uint64_t);
+        // staging slots, two mbarriers, twiddle rows of both plans and the kinetic x factors
+        const size_t smem = 128 + 2 * size_t(L) * W * sizeof(Cx<float>) + 2 * sizeof(uint64_t) +
+                            3 * size_t(L) * sizeof(Cx<float>);
         auto kern = fft_strided_staged_kernel<P, Q, W, OP>;
         static int blocks_per_sm = 0;
         if (blocks_per_sm == 0) {

@@ -34,7 +34,8 @@ namespace wfs {
 //             a contiguous axis) finds the small angles of each k2 in a few lines;
 //   TW_ROW:   tw[t*Q1 + k2] (tw = the plan's row block); a warp that spans one or
 //             two t (strided axes) reads its contiguous row, two twiddles per 16 bytes.
-constexpr int TW_ANGLE = 0, TW_ROW = 1;
+//   TW_ROW_SMEM: TW_ROW with the rows in shared memory (plain loads instead of __ldg).
+constexpr int TW_ANGLE = 0, TW_ROW = 1, TW_ROW_SMEM = 2;
 // Row block of the plan (P1, Q1) in an axis table whose own plan is (P, Q).
 template <int P1, int Q1, int P, int Q, typename R>
 __device__ __forceinline__ const Cx<R>* tw_rows(const Cx<R>* tw) {
@@ -46,15 +47,16 @@ __device__ __forceinline__ void two_stage(Cx<R> (&a_in)[Q1], Cx<R> (&a_out)[P1],
     if (t < P1) {
         dft<Q1, SIGN, R>(a_in);
         auto apply = [&](int k2, Cx<R> w) { a_in[k2] = (SIGN < 0) ? cmul(a_in[k2], w) : cmulc(a_in[k2], w); };
-        if constexpr (TWL == TW_ROW && sizeof(Cx<R>) == 8 && Q1 % 2 == 0) {
+        if constexpr ((TWL == TW_ROW || TWL == TW_ROW_SMEM) && sizeof(Cx<R>) == 8 && Q1 % 2 == 0) {
             const Cx<R>* row = tw + t * Q1;
 #pragma unroll
             for (int j = 0; j < Q1 / 2; ++j) {
-                const float4 w2 = __ldg(reinterpret_cast<const float4*>(row) + j);
+                const float4 w2 = (TWL == TW_ROW) ? __ldg(reinterpret_cast<const float4*>(row) + j)
+                                                  : reinterpret_cast<const float4*>(row)[j];
                 if (j > 0) apply(2 * j, mk<R>(w2.x, w2.y));
                 apply(2 * j + 1, mk<R>(w2.z, w2.w));
             }
-        } else if constexpr (TWL == TW_ROW) {
+        } else if constexpr (TWL == TW_ROW || TWL == TW_ROW_SMEM) {
             const Cx<R>* row = tw + t * Q1;
 #pragma unroll
             for (int k2 = 1; k2 < Q1; ++k2) apply(k2, row[k2]);
@@ -278,6 +280,10 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_STAGED)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Cx<R>* stage = reinterpret_cast<Cx<R>*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));  // [2][L][W]
     uint64_t* bars = reinterpret_cast<uint64_t*>(stage + 2 * L * W);
+    // the two plans' twiddle rows and the kinetic x factors, copied once per CTA: every thread
+    // keeps its row t for all items, and shared-memory reads beat L1 for them (x pass at 256^3:
+    // 59.5 us against 60.5 us through L1)
+    Cx<R>* tsm = reinterpret_cast<Cx<R>*>(bars + 2);  // [P*Q forward rows][Q*P inverse rows][L x factors]
     const int tid = threadIdx.x, c = tid % W, t = tid / W;
     const int rs = int(a.row_stride);
     if (tid == 0) {
@@ -285,7 +291,20 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_STAGED)
         mbar_init(smem_addr(&bars[1]), 1);
         mbar_init_fence();
     }
+    {
+        const Cx<R>* twf = tw_rows<P, Q, P, Q>(a.tw);
+        const Cx<R>* twi = tw_rows<Q, P, P, Q>(a.tw);
+        for (int i = tid; i < L; i += blockDim.x) {
+            tsm[i] = twf[i];
+            tsm[L + i] = twi[i];
+            if constexpr (OP == OP_KIN) tsm[2 * L + i] = a.k_row[i];
+        }
+    }
     __syncthreads();
+    constexpr int TWM = TW_ROW_SMEM;
+    const Cx<R>* tw_f = tsm;
+    const Cx<R>* tw_i = tsm + L;
+    const Cx<R>* k_row = tsm + 2 * L;
     bool expired = false;
     auto issue = [&](int64_t item, int slot) {  // thread 0 only
         if (expired) return;
@@ -320,22 +339,22 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_STAGED)
             for (int i = 0; i < Q; ++i) a1[i] = src[(t + P * i) * W];
         }
         if constexpr (OP == OP_PLAIN) {
-            if (a.dir < 0) two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
-            else two_stage<P, Q, +1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
+            if (a.dir < 0) two_stage<P, Q, -1, TWM>(a1, a2, sm, tw_f, t, sidx_f);
+            else two_stage<P, Q, +1, TWM>(a1, a2, sm, tw_f, t, sidx_f);
             if (active && t < Q) {
 #pragma unroll
                 for (int kk = 0; kk < P; ++kk) base[(t + Q * kk) * rs] = scale(a2[kk], a.scale);
             }
         } else {  // OP_KIN
-            two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(a.tw), t, sidx_f);
+            two_stage<P, Q, -1, TWM>(a1, a2, sm, tw_f, t, sidx_f);
             if (t < Q) {
                 Cx<R> cf = mk<R>(R(0), R(0));
                 if (active) cf = scale(cmul(a.k_c1[col / a.c2n], a.k_c2[col % a.c2n]), a.scale);
 #pragma unroll
-                for (int kk = 0; kk < P; ++kk) a2[kk] = cmul(a2[kk], cmul(a.k_row[t + Q * kk], cf));
+                for (int kk = 0; kk < P; ++kk) a2[kk] = cmul(a2[kk], cmul(k_row[t + Q * kk], cf));
             }
             __syncthreads();
-            two_stage<Q, P, +1, TW_ROW>(a2, a1, sm, tw_rows<Q, P, P, Q>(a.tw), t, sidx_i);
+            two_stage<Q, P, +1, TWM>(a2, a1, sm, tw_i, t, sidx_i);
             if (active && t < P) {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) base[(t + P * i) * rs] = a1[i];
