@@ -64,8 +64,9 @@ __device__ __forceinline__ Cx<double> ld_stream<double>(const Cx<double>* p) {
     return mk<double>(v.x, v.y);
 }
 
-// One y-pencil tile (LY rows x W contiguous z columns) of the plane, in place.
-template <typename R, int P, int Q, int W, int SIGN>
+// One y-pencil tile (LY rows x W contiguous z columns) of the plane, in place. tw is the axis
+// table (TWL = TW_ROW) or, with TWL = TW_ROW_SMEM, the plan's row block in shared memory.
+template <typename R, int P, int Q, int W, int SIGN, int TWL = TW_ROW>
 __device__ __forceinline__ void plane_y_tile(Cx<R>* plane, int nz, int tile, const Cx<R>* tw, R sc, Cx<R>* sm, int tid,
                                              int nthreads) {
     constexpr int T = cmax(P, Q);
@@ -80,7 +81,8 @@ __device__ __forceinline__ void plane_y_tile(Cx<R>* plane, int nz, int tile, con
         for (int i = 0; i < Q; ++i) a1[i] = active ? ld_l2<R>(base + int64_t(t + P * i) * nz) : mk<R>(R(0), R(0));
     }
     auto sidx = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
-    two_stage<P, Q, SIGN, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(tw), in_block ? t : T, sidx);
+    const Cx<R>* rows = (TWL == TW_ROW) ? tw_rows<P, Q, P, Q>(tw) : tw;
+    two_stage<P, Q, SIGN, TWL>(a1, a2, sm, rows, in_block ? t : T, sidx);
     if (active && t < Q) {
 #pragma unroll
         for (int k = 0; k < P; ++k) st_l2<R>(base + int64_t(t + Q * k) * nz, scale(a2[k], sc));
@@ -124,7 +126,7 @@ __device__ __forceinline__ void plane_z_tile(Cx<R>* plane, const Cx<R>* eplane, 
     }
 }
 
-template <typename R, int LY, int LZ, int CL, int NT>
+template <typename R, int LY, int LZ, int CL, int NT, bool TSM = false>
 __global__ void __launch_bounds__(NT, WFS_MINB_PLANE) plane_step_kernel(const PlaneArgs<R> a) {
     constexpr int PY = PlanOf<LY>::P, QY = PlanOf<LY>::Q, TY = cmax(PY, QY);
     constexpr int PZ = PlanOf<LZ>::P, QZ = PlanOf<LZ>::Q, TZ = cmax(PZ, QZ);
@@ -157,33 +159,64 @@ __global__ void __launch_bounds__(NT, WFS_MINB_PLANE) plane_step_kernel(const Pl
             }
         }
     };
+    // TSM: the y plan's twiddle rows and the z angle table, copied once per CTA behind the
+    // transpose buffer; every tile of the CTA reads them from shared memory instead of L1
+    constexpr int RSZ = cmax(QZ * (PZ + 1), PZ * (QZ + 1));
+    constexpr int TWL_Y = TSM ? TW_ROW_SMEM : TW_ROW;
+    const Cx<R>* tw_y = a.tw_y;
+    const Cx<R>* tw_z = a.tw_z;
+    if constexpr (TSM) {
+        Cx<R>* ty = sm + cmax(LY * WY, WZ * RSZ);
+        Cx<R>* tz = ty + PY * QY;
+        const Cx<R>* rows = tw_rows<PY, QY, PY, QY>(a.tw_y);
+        for (int i = tid; i < PY * QY; i += NT) ty[i] = rows[i];
+        for (int i = tid; i < LZ; i += NT) tz[i] = a.tw_z[i];
+        __syncthreads();
+        tw_y = ty;
+        tw_z = tz;
+    }
     for (int tile = rank; tile < ntile_y; tile += CL) {
-        plane_y_tile<R, PY, QY, WY, +1>(plane, LZ, tile, a.tw_y, a.scale_y, sm, tid, NT);
+        plane_y_tile<R, PY, QY, WY, +1, TWL_Y>(plane, LZ, tile, tw_y, a.scale_y, sm, tid, NT);
         __syncthreads();
     }
     prefetch_phase();
     if constexpr (CL > 1) cg::this_cluster().sync(); else __syncthreads();
     for (int tile = rank; tile < ntile_z; tile += CL) {
-        plane_z_tile<R, PZ, QZ, WZ>(plane, eplane, LY, tile, a.tw_z, a.scale_z, sm, tid);
+        plane_z_tile<R, PZ, QZ, WZ>(plane, eplane, LY, tile, tw_z, a.scale_z, sm, tid);
         __syncthreads();
     }
     if constexpr (CL > 1) cg::this_cluster().sync(); else __syncthreads();
     for (int tile = rank; tile < ntile_y; tile += CL) {
-        plane_y_tile<R, PY, QY, WY, -1>(plane, LZ, tile, a.tw_y, a.scale_y, sm, tid, NT);
+        plane_y_tile<R, PY, QY, WY, -1, TWL_Y>(plane, LZ, tile, tw_y, a.scale_y, sm, tid, NT);
         __syncthreads();
     }
 }
 
-template <typename R, int LY, int LZ, int CL>
+// The plane pass reads its twiddles from shared memory (copied once per CTA);
+// WFS_PLANE_SMEM_TABLES=0 in the environment reads them through L1 (for A/B timing).
+inline bool plane_smem_tables_enabled() {
+    static const int on = [] {
+        const char* e = getenv("WFS_PLANE_SMEM_TABLES");
+        return (e && e[0] == '0') ? 0 : 1;
+    }();
+    return on != 0;
+}
+
+template <typename R, int LY, int LZ, int CL, bool TSM_ON = true>
 cudaError_t run_plane(const PlaneArgs<R>& a, int64_t nplanes, cudaStream_t s) {
+    // complex64 only: the tables of a complex128 plane would cost the third CTA per SM
+    constexpr bool TSM = TSM_ON && sizeof(R) == 4;
+    if constexpr (TSM) {
+        if (!plane_smem_tables_enabled()) return run_plane<R, LY, LZ, CL, false>(a, nplanes, s);
+    }
     constexpr int PY = PlanOf<LY>::P, QY = PlanOf<LY>::Q, TY = cmax(PY, QY);
     constexpr int PZ = PlanOf<LZ>::P, QZ = PlanOf<LZ>::Q, TZ = cmax(PZ, QZ);
     constexpr int WY = StridedW<R, TY>::value;
     constexpr int WZ = ContigW<R, TZ>::value;
     constexpr int NT = cmax(TY * WY, TZ * WZ);
     constexpr int RSZ = cmax(QZ * (PZ + 1), PZ * (QZ + 1));
-    const size_t smem = sizeof(Cx<R>) * size_t(cmax(LY * WY, WZ * RSZ));
-    auto kern = plane_step_kernel<R, LY, LZ, CL, NT>;
+    const size_t smem = sizeof(Cx<R>) * (size_t(cmax(LY * WY, WZ * RSZ)) + (TSM ? size_t(PY * QY + LZ) : 0));
+    auto kern = plane_step_kernel<R, LY, LZ, CL, NT, TSM>;
     static bool attr_set = false;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
