@@ -164,47 +164,82 @@ def _f32(x):
     return np.float32(x)
 
 
-def wall_frame(normal, slit_rotation_radian):
-    """Host-side frame of a potential wall, float32 arithmetic.
+def fma32(a, b, c):
+    """Fused multiply-add in float32, correctly rounded: round(a*b + c) with one rounding.
 
-    Restates potential_wall.cu:39-45 and common.cu:348-369 (rotate_vector):
-    up = (0,1,0), replaced by (0,1,1) when |n.up| > 0.99 (the reference only
-    sets up.x = 0 and up.z = 1); right = normalize(cross(n, up)) rotated by
-    slit_rotation_radian around n. cos/sin of the half angle are taken in
-    float64 and rounded to float32.
+    The reference's kernels are compiled with contraction on (NVRTC's default), so
+    its compiler fuses a product into the add or subtract that consumes it. a*b is
+    exact in float64; the float64 sum is corrected with an error-free transformation
+    (TwoSum) where it lands exactly halfway between two float32 values.
+    """
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    c = np.asarray(c, np.float32)
+    p = a.astype(np.float64) * b.astype(np.float64)
+    c64 = c.astype(np.float64)
+    s = p + c64
+    bb = s - p
+    e = (p - (s - bb)) + (c64 - bb)
+    r = s.astype(np.float32)
+    r64 = r.astype(np.float64)
+    other = np.where(s > r64, np.nextafter(r, np.float32(np.inf)), np.nextafter(r, np.float32(-np.inf)))
+    mid = (r64 != s) & (np.abs(s - r64) == np.abs(other.astype(np.float64) - s)) & (e != 0)
+    pick = np.where((e > 0) == (other > r), other, r)
+    return np.where(mid, pick, r).astype(np.float32)
+
+
+def _mul32(a, b):
+    return (np.asarray(a, np.float32) * np.asarray(b, np.float32)).astype(np.float32)
+
+
+def dot3_contracted(a, b):
+    """a.x*b.x + a.y*b.y + a.z*b.z as the reference's compiled dot() evaluates it:
+    the first product fused into the first sum, the third into the second,
+    fma(a.z, b.z, fma(a.x, b.x, a.y*b.y)) (common.cu:65-68)."""
+    return fma32(a[2], b[2], fma32(a[0], b[0], _mul32(a[1], b[1])))
+
+
+def wall_frame(normal, slit_rotation_radian):
+    """Float32 frame of a potential wall as the reference's device code computes it.
+
+    Restates potential_wall.cu:39-45 with common.cu:70-77 (cross), :220-223
+    (normalize) and :348-369 (rotate_vector), with the fused multiply-adds its
+    compiler forms: in a sum or difference of two products the first product is
+    fused (fma(x0, y0, +-x1*y1)); a product added to an earlier sum is fused
+    into it. up = (0,1,0), or (0,1,1) when |n.up| > 0.99 (the reference sets
+    up.x = 0 and up.z = 1); right = normalize(cross(n, up)) rotated by
+    slit_rotation_radian around n; cos/sin of the half angle are the float32
+    roundings of the exact values.
     """
     n = np.asarray(normal, dtype=np.float64)
     n = (n / math.sqrt(float(np.dot(n, n)))).astype(np.float32)  # sources/potential.py:180
     up = np.array([0.0, 1.0, 0.0], dtype=np.float32)
-    nd = _f32(_f32(n[0] * up[0]) + _f32(n[1] * up[1])) + _f32(n[2] * up[2])
-    if abs(float(nd)) > 0.99:
+    if abs(float(dot3_contracted(n, up))) > 0.99:
         up = np.array([0.0, 1.0, 1.0], dtype=np.float32)
     c = np.array([
-        _f32(n[1] * up[2]) - _f32(n[2] * up[1]),
-        _f32(n[2] * up[0]) - _f32(n[0] * up[2]),
-        _f32(n[0] * up[1]) - _f32(n[1] * up[0]),
+        fma32(n[1], up[2], -_mul32(n[2], up[1])),
+        fma32(n[2], up[0], -_mul32(n[0], up[2])),
+        fma32(n[0], up[1], -_mul32(n[1], up[0])),
     ], dtype=np.float32)
-    cc = _f32(_f32(_f32(c[0] * c[0]) + _f32(c[1] * c[1])) + _f32(c[2] * c[2]))
-    ln = np.float32(math.sqrt(float(cc)))
+    ln = np.sqrt(dot3_contracted(c, c)).astype(np.float32)
     right = (c / ln).astype(np.float32)
     half = _f32(_f32(slit_rotation_radian) / _f32(2.0))
     q0 = _f32(math.cos(float(half)))
     s = _f32(math.sin(float(half)))
-    q1, q2, q3 = _f32(s * n[0]), _f32(s * n[1]), _f32(s * n[2])
+    q1, q2, q3 = _mul32(s, n[0]), _mul32(s, n[1]), _mul32(s, n[2])
+    two = _f32(2.0)
     Q = np.zeros((3, 3), dtype=np.float32)
-    Q[0, 0] = _f32(_f32(_f32(q0 * q0) + _f32(q1 * q1)) - _f32(q2 * q2)) - _f32(q3 * q3)
-    Q[0, 1] = _f32(2.0) * _f32(_f32(q1 * q2) - _f32(q0 * q3))
-    Q[0, 2] = _f32(2.0) * _f32(_f32(q1 * q3) + _f32(q0 * q2))
-    Q[1, 0] = _f32(2.0) * _f32(_f32(q2 * q1) + _f32(q0 * q3))
-    Q[1, 1] = _f32(_f32(_f32(q0 * q0) - _f32(q1 * q1)) + _f32(q2 * q2)) - _f32(q3 * q3)
-    Q[1, 2] = _f32(2.0) * _f32(_f32(q2 * q3) - _f32(q0 * q1))
-    Q[2, 0] = _f32(2.0) * _f32(_f32(q3 * q1) - _f32(q0 * q2))
-    Q[2, 1] = _f32(2.0) * _f32(_f32(q3 * q2) + _f32(q0 * q1))
-    Q[2, 2] = _f32(_f32(_f32(q0 * q0) - _f32(q1 * q1)) - _f32(q2 * q2)) + _f32(q3 * q3)
-    rr = np.array([
-        _f32(_f32(_f32(Q[i, 0] * right[0]) + _f32(Q[i, 1] * right[1])) + _f32(Q[i, 2] * right[2]))
-        for i in range(3)
-    ], dtype=np.float32)
+    Q[0, 0] = fma32(-q3, q3, fma32(-q2, q2, fma32(q0, q0, _mul32(q1, q1))))
+    Q[0, 1] = _mul32(two, fma32(q1, q2, -_mul32(q0, q3)))
+    Q[0, 2] = _mul32(two, fma32(q1, q3, _mul32(q0, q2)))
+    Q[1, 0] = _mul32(two, fma32(q2, q1, _mul32(q0, q3)))
+    Q[1, 1] = fma32(-q3, q3, fma32(q2, q2, fma32(q0, q0, -_mul32(q1, q1))))
+    Q[1, 2] = _mul32(two, fma32(q2, q3, -_mul32(q0, q1)))
+    Q[2, 0] = _mul32(two, fma32(q3, q1, -_mul32(q0, q2)))
+    Q[2, 1] = _mul32(two, fma32(q3, q2, _mul32(q0, q1)))
+    Q[2, 2] = fma32(q3, q3, fma32(-q2, q2, fma32(q0, q0, -_mul32(q1, q1))))
+    rr = np.array([fma32(Q[i, 2], right[2], fma32(Q[i, 0], right[0], _mul32(Q[i, 1], right[1]))) for i in range(3)],
+                  dtype=np.float32)
     return n, rr
 
 
@@ -227,8 +262,10 @@ def add_potential_wall(V, dx, wall: Wall):
     """V += wall (real part), restating sources/cuda_kernels/potential_wall.cu:4-83.
 
     r = dx * (voxel - 0.5 N); d = |n.(r-c)|; dR = |right.(r-c)|; slits leave
-    V untouched; plateau adds U, slope adds U*(1-(d-p/2)/s)^e.
-    All arithmetic in float32 without fused multiply-adds.
+    V untouched; plateau adds U, slope adds U*(1-(d-p/2)/s)^e. Float32
+    arithmetic with the reference compiler's fused multiply-adds (the dot
+    products as in ``dot3_contracted``; ``sp*1.5 -+ sw*0.5`` fuses the first
+    product), which decide the voxels that lie exactly on a plateau or slit edge.
     """
     n = V.shape
     f = np.float32
@@ -239,11 +276,12 @@ def add_potential_wall(V, dx, wall: Wall):
     for a in range(3):
         v = np.arange(n[a], dtype=np.float32)
         coords.append((d32[a] * (v - f(0.5) * f(n[a]))).astype(np.float32))
-    ax = (coords[0] - c[0])[:, None, None]
-    ay = (coords[1] - c[1])[None, :, None]
-    az = (coords[2] - c[2])[None, None, :]
-    d = np.abs((nrm[0] * ax + nrm[1] * ay) + nrm[2] * az).astype(np.float32)
-    dR = np.abs((right[0] * ax + right[1] * ay) + right[2] * az).astype(np.float32)
+    shape = tuple(int(x) for x in n)
+    ax = np.broadcast_to((coords[0] - c[0]).astype(np.float32)[:, None, None], shape)
+    ay = np.broadcast_to((coords[1] - c[1]).astype(np.float32)[None, :, None], shape)
+    az = np.broadcast_to((coords[2] - c[2]).astype(np.float32)[None, None, :], shape)
+    d = np.abs(fma32(nrm[2], az, fma32(nrm[0], ax, _mul32(nrm[1], ay))))
+    dR = np.abs(fma32(right[2], az, fma32(right[0], ax, _mul32(right[1], ay))))
     sw = f(wall.slit_width_bohr_radii)
     sp = f(wall.slit_spacing_bohr_radii)
     half = f(0.5)
@@ -256,7 +294,7 @@ def add_potential_wall(V, dx, wall: Wall):
         skip = (dR < sw * half) | ((dR > sp - sw * half) & (dR < sp + sw * half))
     elif sc == 4:
         skip = ((dR > (sp - sw) * half) & (dR < (sp + sw) * half)) | (
-            (dR > sp * f(1.5) - sw * half) & (dR < sp * f(1.5) + sw * half))
+            (dR > fma32(sp, f(1.5), -_mul32(sw, half))) & (dR < fma32(sp, f(1.5), _mul32(sw, half))))
     else:
         skip = np.zeros(d.shape, dtype=bool)
     U = f(wall.potential_hartree)
@@ -286,10 +324,23 @@ class Absorbing:
     exponent_neg: tuple = (2.0, 2.0, 2.0)
 
 
+def _atan32(x):
+    """float32 atan, correctly rounded (evaluated in float64)."""
+    return np.arctan(np.asarray(x, np.float32).astype(np.float64)).astype(np.float32)
+
+
+def _pow32(a, b):
+    """float32 pow, correctly rounded (evaluated in float64)."""
+    return np.power(np.asarray(a, np.float32).astype(np.float64), np.asarray(b, np.float32).astype(np.float64)).astype(
+        np.float32)
+
+
 def _mix(xyz, u, v):
-    """common.cu:394-397 — xyz.z*v + (1-v)*(xyz.y*u + xyz.x*(1-u))."""
+    """common.cu:394-397 — xyz.z*v + (1-v)*(xyz.y*u + xyz.x*(1-u)), with the
+    compiler's fusions: fma(z, v, (1-v)*fma(y, u, x*(1-u)))."""
     f = np.float32
-    return (xyz[2] * v + (f(1.0) - v) * (xyz[1] * u + xyz[0] * (f(1.0) - u))).astype(np.float32)
+    inner = fma32(xyz[1], u, _mul32(xyz[0], (f(1.0) - u)))
+    return fma32(xyz[2], v, _mul32((f(1.0) - v), inner))
 
 
 def absorbing_potential_imag(n, dx, ab: Absorbing):
@@ -298,6 +349,9 @@ def absorbing_potential_imag(n, dx, ab: Absorbing):
     26 regions (8 corners, 12 edges, 6 faces) tested in the reference's order,
     first match wins; quirks kept (edges 10, 12 and 20 blend maxD with u=0).
     Returns the float32 ramp U(r) that the reference adds as V += i*U.
+    Float32 arithmetic with the reference compiler's fused multiply-adds: the
+    voxel position dx*v - (0.5 N) dx fuses the first product, sqrt(a*a + b*b) is
+    sqrt(fma(a, a, b*b)), lengths follow ``dot3_contracted`` and blends ``_mix``.
     """
     f = np.float32
     d32 = np.array(dx, dtype=np.float32)
@@ -313,7 +367,7 @@ def absorbing_potential_imag(n, dx, ab: Absorbing):
     rr = []
     for a in range(3):
         v = np.arange(n[a], dtype=np.float32)
-        rr.append((d32[a] * v - (f(0.5) * N[a]) * d32[a]).astype(np.float32))
+        rr.append(fma32(d32[a], v, -box_half[a]))
     rx = rr[0][:, None, None]
     ry = rr[1][None, :, None]
     rz = rr[2][None, None, :]
@@ -332,10 +386,10 @@ def absorbing_potential_imag(n, dx, ab: Absorbing):
     abst = np.abs(top)
 
     def L3(a, b, c):
-        return np.sqrt((a * a + b * b) + c * c).astype(np.float32)
+        return np.sqrt(dot3_contracted((a, b, c), (a, b, c))).astype(np.float32)
 
     def ramp(mask, dist, maxD, expo, pot):
-        val = np.power(np.maximum(dist - off, zero) / maxD, expo).astype(np.float32) * pot
+        val = _pow32(np.maximum(dist - off, zero) / maxD, expo).astype(np.float32) * pot
         out[mask] = val.astype(np.float32)
 
     def corner(cond, a_num, a_den, b_num, b_h1, b_h2, sel_abs, sel_e, sel_p, dvec):
@@ -343,9 +397,9 @@ def absorbing_potential_imag(n, dx, ab: Absorbing):
         if not np.any(m):
             return m
         an = a_num[m]; ad = a_den[m]
-        u = (np.arctan(an / ad) / pi * f(2.0)).astype(np.float32)
+        u = (_atan32(an / ad) / pi * f(2.0)).astype(np.float32)
         h1 = b_h1[m]; h2 = b_h2[m]
-        v = (np.arctan(b_num[m] / np.sqrt(h1 * h1 + h2 * h2)) / pi * f(2.0)).astype(np.float32)
+        v = (_atan32(b_num[m] / np.sqrt(fma32(h1, h1, _mul32(h2, h2)))) / pi * f(2.0)).astype(np.float32)
         maxd_xyz = [box_half[i] - (sel_abs[i] + off) for i in range(3)]
         maxD = _mix(maxd_xyz, u, v)
         expo = _mix(sel_e, u, v)
@@ -378,7 +432,7 @@ def absorbing_potential_imag(n, dx, ab: Absorbing):
         m = cond & ~done
         if not np.any(m):
             return
-        ang = (np.arctan(num[m] / den[m]) / pi * f(2.0)).astype(np.float32)
+        ang = (_atan32(num[m] / den[m]) / pi * f(2.0)).astype(np.float32)
         maxd_xyz = [box_half[i] - (sel_abs[i] + sel_off[i]) for i in range(3)]
         if use_u:   # blend in x/y with u = ang, v = 0
             maxD = _mix(maxd_xyz, ang, zero)
@@ -426,7 +480,7 @@ def absorbing_potential_imag(n, dx, ab: Absorbing):
         m = cond & ~done
         if not np.any(m):
             return
-        val = np.power(np.maximum(dist[m] - off, zero) / maxD, expo).astype(np.float32) * pot
+        val = _pow32(np.maximum(dist[m] - off, zero) / maxD, expo).astype(np.float32) * pot
         out[m] = val.astype(np.float32)
         done[m] = True
 

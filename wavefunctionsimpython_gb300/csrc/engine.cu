@@ -689,54 +689,8 @@ int wfs_potential_clear(wfs_handle* h) {
 int wfs_potential_add_wall(wfs_handle* h, const wfs_wall* w) {
     if (!h) return dispatch_err(h);
     if (!w) return set_err(h, WFS_ERR_ARG, "null wall");
-    // frame: potential_wall.cu:39-45 and common.cu:348-369, float32 on the host
-    double nn = std::sqrt(w->normal[0] * w->normal[0] + w->normal[1] * w->normal[1] + w->normal[2] * w->normal[2]);
-    if (!(nn > 0)) return set_err(h, WFS_ERR_ARG, "wall normal has zero length");
-    volatile float n[3] = {float(w->normal[0] / nn), float(w->normal[1] / nn), float(w->normal[2] / nn)};
-    volatile float up[3] = {0.f, 1.f, 0.f};
-    volatile float t0 = n[0] * up[0];
-    volatile float t1 = n[1] * up[1];
-    volatile float t2 = n[2] * up[2];
-    volatile float nd = t0 + t1;
-    nd = nd + t2;
-    if (std::fabs(float(nd)) > 0.99f) { up[0] = 0.f; up[2] = 1.f; }
-    auto mul = [](float a, float b) { volatile float r = a * b; return float(r); };
-    auto add = [](float a, float b) { volatile float r = a + b; return float(r); };
-    auto sub = [](float a, float b) { volatile float r = a - b; return float(r); };
-    float c[3] = {sub(mul(n[1], up[2]), mul(n[2], up[1])), sub(mul(n[2], up[0]), mul(n[0], up[2])),
-                  sub(mul(n[0], up[1]), mul(n[1], up[0]))};
-    float cc = add(add(mul(c[0], c[0]), mul(c[1], c[1])), mul(c[2], c[2]));
-    float ln = float(std::sqrt(double(cc)));
-    if (!(ln > 0)) return set_err(h, WFS_ERR_ARG, "degenerate wall frame");
-    float right[3];
-    for (int i = 0; i < 3; ++i) { volatile float r = c[i] / ln; right[i] = r; }
-    volatile float half = float(w->slit_rotation) / 2.0f;
-    float q0 = float(std::cos(double(half)));
-    float s = float(std::sin(double(half)));
-    float q1 = mul(s, n[0]), q2 = mul(s, n[1]), q3 = mul(s, n[2]);
-    float Q[3][3];
-    Q[0][0] = sub(sub(add(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
-    Q[0][1] = mul(2.f, sub(mul(q1, q2), mul(q0, q3)));
-    Q[0][2] = mul(2.f, add(mul(q1, q3), mul(q0, q2)));
-    Q[1][0] = mul(2.f, add(mul(q2, q1), mul(q0, q3)));
-    Q[1][1] = sub(add(sub(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
-    Q[1][2] = mul(2.f, sub(mul(q2, q3), mul(q0, q1)));
-    Q[2][0] = mul(2.f, sub(mul(q3, q1), mul(q0, q2)));
-    Q[2][1] = mul(2.f, add(mul(q3, q2), mul(q0, q1)));
-    Q[2][2] = add(sub(sub(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
-    float rr[3];
-    for (int i = 0; i < 3; ++i) rr[i] = add(add(mul(Q[i][0], right[0]), mul(Q[i][1], right[1])), mul(Q[i][2], right[2]));
     WallDev wd;
-    wd.U = float(w->potential_hartree);
-    wd.cx = float(w->center[0]); wd.cy = float(w->center[1]); wd.cz = float(w->center[2]);
-    wd.nx = n[0]; wd.ny = n[1]; wd.nz = n[2];
-    wd.rx = rr[0]; wd.ry = rr[1]; wd.rz = rr[2];
-    wd.plateau = float(w->plateau_thickness);
-    wd.slope = float(w->slope_thickness);
-    wd.slope_exp = float(w->slope_exponent);
-    wd.slit_count = w->slit_count < 0 ? 0 : (w->slit_count > 4 ? 4 : w->slit_count);
-    wd.slit_spacing = float(w->slit_spacing);
-    wd.slit_width = float(w->slit_width);
+    if (!wall_frame(w, wd)) return set_err(h, WFS_ERR_ARG, "wall normal has zero length or a value is not finite");
     float dx[3] = {float(h->dx[0]), float(h->dx[1]), float(h->dx[2])};
     CK(launch_wall(h->V, h->n, dx, wd, h->stream));
     h->ephase_valid = false;

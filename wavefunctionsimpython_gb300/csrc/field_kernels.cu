@@ -2,9 +2,14 @@
 //
 // The potential builders restate the reference's float32 formulas
 // (sources/cuda_kernels/potential_wall.cu:4-83, absorbing_potential.cu:3-307)
-// with explicitly rounded multiplies and adds (__fmul_rn/__fadd_rn), so that
-// no fused multiply-add changes a rounding and the real-valued geometry is
-// reproducible on any host that evaluates the same float32 expression.
+// with every rounding spelled out: separately rounded multiplies and adds
+// (__fmul_rn/__fadd_rn) where the reference's compiled code rounds them, and a
+// fused multiply-add (__fmaf_rn) exactly where its compiler contracts a product
+// into the add or subtract that consumes it. The reference is compiled with
+// contraction on (NVRTC's default); in a sum or difference of two products the
+// first product is fused, and a product added to an earlier result is fused into
+// it. These fusions decide the voxels that lie exactly on a wall's plateau or
+// slit edge, so the potential matches the reference's bit for bit.
 #include "fft_kernels.cuh"
 
 namespace wfs {
@@ -13,12 +18,46 @@ __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); 
 __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
 
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// common.cu:65-68 as compiled: fma(a.z, b.z, fma(a.x, b.x, a.y*b.y))
+__device__ __forceinline__ float dot3c(float ax, float ay, float az, float bx, float by, float bz) {
+    return fma_(az, bz, fma_(ax, bx, fm(ay, by)));
+}
+
 // ---------------------------------------------------------------------------
-// Potential wall — potential_wall.cu:30-82. The frame (normal, rotated right)
-// is computed once on the host.
+// Potential wall — potential_wall.cu:30-82. Each thread forms the wall's frame
+// (potential_wall.cu:39-45 with common.cu:70-77 cross, :220-223 normalize and
+// :348-369 rotate_vector) as the reference's device code does, with the same
+// cosf/sinf of the half angle and the same fused multiply-adds.
 // ---------------------------------------------------------------------------
+__device__ void wall_right(const WallDev& w, float r[3]) {
+    float upx = 0.f, upy = 1.f, upz = 0.f;
+    if (fabsf(dot3c(w.nx, w.ny, w.nz, upx, upy, upz)) > 0.99f) { upx = 0.f; upz = 1.f; }
+    const float c0 = fma_(w.ny, upz, -fm(w.nz, upy));
+    const float c1 = fma_(w.nz, upx, -fm(w.nx, upz));
+    const float c2 = fma_(w.nx, upy, -fm(w.ny, upx));
+    const float ln = __fsqrt_rn(dot3c(c0, c1, c2, c0, c1, c2));
+    const float rt[3] = {__fdiv_rn(c0, ln), __fdiv_rn(c1, ln), __fdiv_rn(c2, ln)};
+    const float half = __fdiv_rn(w.rot, 2.0f);
+    const float q0 = cosf(half), sh = sinf(half);
+    const float q1 = fm(sh, w.nx), q2 = fm(sh, w.ny), q3 = fm(sh, w.nz);
+    float Q[3][3];
+    Q[0][0] = fma_(-q3, q3, fma_(-q2, q2, fma_(q0, q0, fm(q1, q1))));
+    Q[0][1] = fm(2.0f, fma_(q1, q2, -fm(q0, q3)));
+    Q[0][2] = fm(2.0f, fma_(q1, q3, fm(q0, q2)));
+    Q[1][0] = fm(2.0f, fma_(q2, q1, fm(q0, q3)));
+    Q[1][1] = fma_(-q3, q3, fma_(q2, q2, fma_(q0, q0, -fm(q1, q1))));
+    Q[1][2] = fm(2.0f, fma_(q2, q3, -fm(q0, q1)));
+    Q[2][0] = fm(2.0f, fma_(q3, q1, -fm(q0, q2)));
+    Q[2][1] = fm(2.0f, fma_(q3, q2, fm(q0, q1)));
+    Q[2][2] = fma_(q3, q3, fma_(-q2, q2, fma_(q0, q0, -fm(q1, q1))));
+    for (int i = 0; i < 3; ++i) r[i] = fma_(Q[i][2], rt[2], fma_(Q[i][0], rt[0], fm(Q[i][1], rt[1])));
+}
+
 __global__ void wall_kernel(float2* __restrict__ V, int nx, int ny, int nz, float dxx, float dxy, float dxz, WallDev w) {
     const int64_t total = int64_t(nx) * ny * nz;
+    float right[3];
+    wall_right(w, right);
     for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total; idx += int64_t(gridDim.x) * blockDim.x) {
         const int z = int(idx % nz);
         const int y = int((idx / nz) % ny);
@@ -27,8 +66,8 @@ __global__ void wall_kernel(float2* __restrict__ V, int nx, int ny, int nz, floa
         const float ry = fm(dxy, fs(float(y), fm(0.5f, float(ny))));
         const float rz = fm(dxz, fs(float(z), fm(0.5f, float(nz))));
         const float ax = fs(rx, w.cx), ay = fs(ry, w.cy), az = fs(rz, w.cz);
-        const float d = fabsf(fa(fa(fm(w.nx, ax), fm(w.ny, ay)), fm(w.nz, az)));
-        const float dR = fabsf(fa(fa(fm(w.rx, ax), fm(w.ry, ay)), fm(w.rz, az)));
+        const float d = fabsf(dot3c(w.nx, w.ny, w.nz, ax, ay, az));
+        const float dR = fabsf(dot3c(right[0], right[1], right[2], ax, ay, az));
         const float sw = w.slit_width, sp = w.slit_spacing;
         bool skip = false;
         switch (w.slit_count) {
@@ -39,7 +78,7 @@ __global__ void wall_kernel(float2* __restrict__ V, int nx, int ny, int nz, floa
                 break;
             case 4:
                 skip = (dR > fm(fs(sp, sw), 0.5f) && dR < fm(fa(sp, sw), 0.5f)) ||
-                       (dR > fs(fm(sp, 1.5f), fm(sw, 0.5f)) && dR < fa(fm(sp, 1.5f), fm(sw, 0.5f)));
+                       (dR > fma_(sp, 1.5f, -fm(sw, 0.5f)) && dR < fma_(sp, 1.5f, fm(sw, 0.5f)));
                 break;
             default: break;
         }
@@ -68,11 +107,17 @@ cudaError_t launch_wall(float2* V, const int n[3], const float dx[3], const Wall
 struct F3 { float x, y, z; };
 __device__ __forceinline__ F3 f3(float a, float b, float c) { return F3{a, b, c}; }
 // common.cu:394-397
+// common.cu:394-397 as compiled: fma(z, w, (1-w) * fma(y, u, x*(1-u)))
 __device__ __forceinline__ float mixf(F3 v, float u, float w) {
-    return fa(fm(v.z, w), fm(fs(1.0f, w), fa(fm(v.y, u), fm(v.x, fs(1.0f, u)))));
+    return fma_(v.z, w, fm(fs(1.0f, w), fma_(v.y, u, fm(v.x, fs(1.0f, u)))));
 }
+// length(): sqrtf(dot(v, v)) (common.cu:215-218)
 __device__ __forceinline__ float len3(float a, float b, float c) {
-    return __fsqrt_rn(fa(fa(fm(a, a), fm(b, b)), fm(c, c)));
+    return __fsqrt_rn(dot3c(a, b, c, a, b, c));
+}
+// sqrtf(a*a + b*b) as compiled: sqrt(fma(a, a, b*b))
+__device__ __forceinline__ float hyp2(float a, float b) {
+    return __fsqrt_rn(fma_(a, a, fm(b, b)));
 }
 __device__ __forceinline__ float ramp(float dist, float off, float maxD, float e, float pot) {
     return fm(powf(__fdiv_rn(fmaxf(fs(dist, off), 0.0f), maxD), e), pot);
@@ -91,9 +136,10 @@ __global__ void absorbing_kernel(float2* __restrict__ V, int nx, int ny, int nz,
         const int z = int(idx % nz);
         const int y = int((idx / nz) % ny);
         const int x = int(idx / (int64_t(ny) * nz));
-        const float rx = fs(fm(dxx, float(x)), fm(fm(0.5f, float(nx)), dxx));
-        const float ry = fs(fm(dxy, float(y)), fm(fm(0.5f, float(ny)), dxy));
-        const float rz = fs(fm(dxz, float(z)), fm(fm(0.5f, float(nz)), dxz));
+        // delta_r * voxel - 0.5 N delta_r, the first product fused
+        const float rx = fma_(dxx, float(x), -box_half.x);
+        const float ry = fma_(dxy, float(y), -box_half.y);
+        const float rz = fma_(dxz, float(z), -box_half.z);
         const float Bx = fs(rx, a.bottom[0]), By = fs(ry, a.bottom[1]), Bz = fs(rz, a.bottom[2]);
         const float Tx = fs(rx, a.top[0]), Ty = fs(ry, a.top[1]), Tz = fs(rz, a.top[2]);
         float pot = 0.0f;
@@ -104,37 +150,37 @@ __global__ void absorbing_kernel(float2* __restrict__ V, int nx, int ny, int nz,
         const float h = 0.0f;
         // corners of the bottom plate
         if (Bx < 0.f && By < 0.f && Bz < 0.f) {
-            float u = ang(By, Bx), v = ang(-Bz, __fsqrt_rn(fa(fm(Bx, Bx), fm(By, By))));
+            float u = ang(By, Bx), v = ang(-Bz, hyp2(Bx, By));
             F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, ab.y, ab.z, off, off, off);
             pot = ramp(len3(Bx, By, Bz), off, mixf(m, u, v), mixf(f3(a.en[0], a.en[1], a.en[2]), u, v), mixf(f3(a.pn[0], a.pn[1], a.pn[2]), u, v));
         } else if (Bx < 0.f && By < 0.f && Tz > 0.f) {
-            float u = ang(By, Bx), v = ang(Tz, __fsqrt_rn(fa(fm(Bx, Bx), fm(By, By))));
+            float u = ang(By, Bx), v = ang(Tz, hyp2(Bx, By));
             F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, ab.y, at.z, off, off, off);
             pot = ramp(len3(Bx, By, Tz), off, mixf(m, u, v), mixf(f3(a.en[0], a.en[1], a.ep[2]), u, v), mixf(f3(a.pn[0], a.pn[1], a.pp[2]), u, v));
         } else if (By < 0.f && Tx > 0.f && Tz > 0.f) {
-            float u = ang(-By, Tx), v = ang(Tz, __fsqrt_rn(fa(fm(Tx, Tx), fm(By, By))));
+            float u = ang(-By, Tx), v = ang(Tz, hyp2(Tx, By));
             F3 m = md(box_half.x, box_half.y, box_half.z, at.x, ab.y, at.z, off, off, off);
             pot = ramp(len3(Tx, By, Tz), off, mixf(m, u, v), mixf(f3(a.ep[0], a.en[1], a.ep[2]), u, v), mixf(f3(a.pp[0], a.pn[1], a.pp[2]), u, v));
         } else if (By < 0.f && Bz < 0.f && Tx > 0.f) {
-            float u = ang(-By, Tx), v = ang(-Bz, __fsqrt_rn(fa(fm(Tx, Tx), fm(By, By))));
+            float u = ang(-By, Tx), v = ang(-Bz, hyp2(Tx, By));
             F3 m = md(box_half.x, box_half.y, box_half.z, at.x, ab.y, ab.z, off, off, off);
             pot = ramp(len3(Tx, By, Bz), off, mixf(m, u, v), mixf(f3(a.ep[0], a.en[1], a.en[2]), u, v), mixf(f3(a.pp[0], a.pn[1], a.pn[2]), u, v));
         }
         // corners of the top plate
         else if (Tx > 0.f && Ty > 0.f && Tz > 0.f) {
-            float u = ang(Ty, Tx), v = ang(Tz, __fsqrt_rn(fa(fm(Tx, Tx), fm(Ty, Ty))));
+            float u = ang(Ty, Tx), v = ang(Tz, hyp2(Tx, Ty));
             F3 m = md(box_half.x, box_half.y, box_half.z, at.x, at.y, at.z, off, off, off);
             pot = ramp(len3(Tx, Ty, Tz), off, mixf(m, u, v), mixf(f3(a.ep[0], a.ep[1], a.ep[2]), u, v), mixf(f3(a.pp[0], a.pp[1], a.pp[2]), u, v));
         } else if (Bz < 0.f && Tx > 0.f && Ty > 0.f) {
-            float u = ang(Ty, Tx), v = ang(-Bz, __fsqrt_rn(fa(fm(Tx, Tx), fm(Ty, Ty))));
+            float u = ang(Ty, Tx), v = ang(-Bz, hyp2(Tx, Ty));
             F3 m = md(box_half.x, box_half.y, box_half.z, at.x, at.y, ab.z, off, off, off);
             pot = ramp(len3(Tx, Ty, Bz), off, mixf(m, u, v), mixf(f3(a.ep[0], a.ep[1], a.en[2]), u, v), mixf(f3(a.pp[0], a.pp[1], a.pn[2]), u, v));
         } else if (Bx < 0.f && Bz < 0.f && Ty > 0.f) {
-            float u = ang(Ty, -Bx), v = ang(-Bz, __fsqrt_rn(fa(fm(Bx, Bx), fm(Ty, Ty))));
+            float u = ang(Ty, -Bx), v = ang(-Bz, hyp2(Bx, Ty));
             F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, at.y, ab.z, off, off, off);
             pot = ramp(len3(Bx, Ty, Bz), off, mixf(m, u, v), mixf(f3(a.en[0], a.ep[1], a.en[2]), u, v), mixf(f3(a.pn[0], a.pp[1], a.pn[2]), u, v));
         } else if (Bx < 0.f && Ty > 0.f && Tz > 0.f) {
-            float u = ang(Ty, -Bx), v = ang(Tz, __fsqrt_rn(fa(fm(Bx, Bx), fm(Ty, Ty))));
+            float u = ang(Ty, -Bx), v = ang(Tz, hyp2(Bx, Ty));
             F3 m = md(box_half.x, box_half.y, box_half.z, ab.x, at.y, at.z, off, off, off);
             pot = ramp(len3(Bx, Ty, Tz), off, mixf(m, u, v), mixf(f3(a.en[0], a.ep[1], a.ep[2]), u, v), mixf(f3(a.pn[0], a.pp[1], a.pp[2]), u, v));
         }

@@ -50,45 +50,18 @@ inline void gaussian_axes(const int n[3], const double dx[3], const double sigma
     }
 }
 
-// Float32 frame of a wall (potential_wall.cu:39-45, common.cu:348-369) with
-// every product and sum rounded separately, as the reference's device code does.
+// Wall parameters for the device (potential_wall.cu:4-83). The normal is
+// normalised in double precision and rounded to float32, as the reference does
+// on the host (sources/potential.py:180); the wall's frame (up, right, the slit
+// rotation) is formed by each thread of wall_kernel in the reference's float32
+// device arithmetic.
 inline bool wall_frame(const wfs_wall* w, WallDev& wd) {
     const double nn = std::sqrt(w->normal[0] * w->normal[0] + w->normal[1] * w->normal[1] + w->normal[2] * w->normal[2]);
-    if (!(nn > 0)) return false;
-    auto mul = [](float a, float b) { volatile float r = a * b; return float(r); };
-    auto add = [](float a, float b) { volatile float r = a + b; return float(r); };
-    auto sub = [](float a, float b) { volatile float r = a - b; return float(r); };
-    const float n[3] = {float(w->normal[0] / nn), float(w->normal[1] / nn), float(w->normal[2] / nn)};
-    float up[3] = {0.f, 1.f, 0.f};
-    const float nd = add(add(mul(n[0], up[0]), mul(n[1], up[1])), mul(n[2], up[2]));
-    if (std::fabs(nd) > 0.99f) { up[0] = 0.f; up[2] = 1.f; }
-    const float c[3] = {sub(mul(n[1], up[2]), mul(n[2], up[1])), sub(mul(n[2], up[0]), mul(n[0], up[2])),
-                        sub(mul(n[0], up[1]), mul(n[1], up[0]))};
-    const float cc = add(add(mul(c[0], c[0]), mul(c[1], c[1])), mul(c[2], c[2]));
-    const float ln = float(std::sqrt(double(cc)));
-    if (!(ln > 0)) return false;
-    float right[3];
-    for (int i = 0; i < 3; ++i) { volatile float r = c[i] / ln; right[i] = r; }
-    volatile float half = float(w->slit_rotation) / 2.0f;
-    const float q0 = float(std::cos(double(half)));
-    const float s = float(std::sin(double(half)));
-    const float q1 = mul(s, n[0]), q2 = mul(s, n[1]), q3 = mul(s, n[2]);
-    float Q[3][3];
-    Q[0][0] = sub(sub(add(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
-    Q[0][1] = mul(2.f, sub(mul(q1, q2), mul(q0, q3)));
-    Q[0][2] = mul(2.f, add(mul(q1, q3), mul(q0, q2)));
-    Q[1][0] = mul(2.f, add(mul(q2, q1), mul(q0, q3)));
-    Q[1][1] = sub(add(sub(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
-    Q[1][2] = mul(2.f, sub(mul(q2, q3), mul(q0, q1)));
-    Q[2][0] = mul(2.f, sub(mul(q3, q1), mul(q0, q2)));
-    Q[2][1] = mul(2.f, add(mul(q3, q2), mul(q0, q1)));
-    Q[2][2] = add(sub(sub(mul(q0, q0), mul(q1, q1)), mul(q2, q2)), mul(q3, q3));
-    float rr[3];
-    for (int i = 0; i < 3; ++i) rr[i] = add(add(mul(Q[i][0], right[0]), mul(Q[i][1], right[1])), mul(Q[i][2], right[2]));
+    if (!(nn > 0) || !std::isfinite(nn) || !std::isfinite(w->slit_rotation)) return false;
     wd.U = float(w->potential_hartree);
     wd.cx = float(w->center[0]); wd.cy = float(w->center[1]); wd.cz = float(w->center[2]);
-    wd.nx = n[0]; wd.ny = n[1]; wd.nz = n[2];
-    wd.rx = rr[0]; wd.ry = rr[1]; wd.rz = rr[2];
+    wd.nx = float(w->normal[0] / nn); wd.ny = float(w->normal[1] / nn); wd.nz = float(w->normal[2] / nn);
+    wd.rot = float(w->slit_rotation);
     wd.plateau = float(w->plateau_thickness);
     wd.slope = float(w->slope_thickness);
     wd.slope_exp = float(w->slope_exponent);

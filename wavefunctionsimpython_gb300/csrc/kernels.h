@@ -110,7 +110,7 @@ bool plane_pass_supported(int ny, int nz);
 
 // ---- field kernels (field_kernels.cu) ----
 struct WallDev {
-    float U, cx, cy, cz, nx, ny, nz, rx, ry, rz;
+    float U, cx, cy, cz, nx, ny, nz, rot;  // rot: slit rotation (radian); the frame is formed on the device
     float plateau, slope, slope_exp, slit_spacing, slit_width;
     int slit_count;
 };
