@@ -13,8 +13,9 @@ Printed JSON line (rank 0):
              no explicit L2 flush is needed between steps);
   e2e        the same metric through the public API with host buffers: psi0 and
              V uploaded from pinned host memory, the run, the series and psi read back;
-  roofline   dominant pass (by device time inside the timed region, per-launch
-             CUDA events): algorithmic bytes per launch / mean launch time vs the
+  roofline   dominant pass (by device time, per-launch CUDA events in a separate
+             untimed run of the same schedule, so no events sit in the timed
+             region): algorithmic bytes per launch / mean launch time vs the
              measured HBM copy bandwidth;
   cpu_baseline  the NumPy oracle on one host core, on a bounded sample of steps.
 
@@ -48,12 +49,7 @@ SIGMA, R0, K0 = (3.0, 3.0, 3.0), (-20.0, 0.0, 0.0), (2.5, 0.0, 0.0)
 ABS_CELLS = 16
 ABS_POT = -50.0
 METRIC = "site-steps/s at 256^3 c64 (split-step, double slit)"
-PROFILE_STRIDE = 10  # per-launch CUDA events on every 10th step of long timed regions
-
-
-def profile_stride(steps):
-    """Event sampling stride: every 10th step of long runs, every step of short ones."""
-    return PROFILE_STRIDE if steps >= 20 * PROFILE_STRIDE else 1
+PROFILE_STEPS = 40  # steps of the separate, untimed run that measures each pass
 
 
 def engine_stream(torch):
@@ -258,8 +254,7 @@ def run_own(args):
     # warm-up (also allocates the observation buffers)
     e.run_split(max(args.warmup, 1), DT, 1.0, OBS_INTERVAL, [box], None)
     torch.cuda.synchronize()
-    e.profile_read(reset=True)
-    e.profile_enable(True, stride=profile_stride(args.steps))
+    e.profile_enable(False)
     launches0 = e.launch_count()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
@@ -272,9 +267,15 @@ def run_own(args):
         barrier(pg)
     ms = start.elapsed_time(stop)
     launches = e.launch_count() - launches0
+    ms = max_over_ranks(pg, ms, device=f"cuda:{dev}" if world > 1 else None)
+    # per-pass device times for the roofline: a separate, untimed run of the same
+    # schedule with CUDA events around every launch (kept out of the timed region)
+    e.profile_read(reset=True)
+    e.profile_enable(True, stride=1)
+    e.run_split(PROFILE_STEPS, DT, 1.0, OBS_INTERVAL, [box], None)
+    torch.cuda.synchronize()
     prof = e.profile_read(reset=True)
     e.profile_enable(False)
-    ms = max_over_ranks(pg, ms, device=f"cuda:{dev}" if world > 1 else None)
     value = world * N ** 3 * args.steps / (ms * 1e-3)
 
     # roofline of the dominant pass
@@ -348,10 +349,9 @@ def run_taylor(args):
     e = Engine((n, n, n), (L,) * 3, device=args.device, stream=stream.cuda_stream)
     e.set_potential(V)
     e.init_gaussian((1.5,) * 3, (5.0, 0.0, 0.0), (0.0, 0.0, 0.0))
-    e.step_taylor(args.warmup, 0.005, 1.0, order, 4)
+    e.step_taylor(max(args.warmup, 1), 0.005, 1.0, order, 4)
     torch.cuda.synchronize()
-    e.profile_read(reset=True)
-    e.profile_enable(True, stride=profile_stride(args.steps))
+    e.profile_enable(False)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(args.device) as clk:
         torch.cuda.synchronize()
@@ -360,7 +360,13 @@ def run_taylor(args):
         stop.record(stream)
         torch.cuda.synchronize()
     ms = start.elapsed_time(stop)
+    # per-term device time from a separate, untimed run with events around each launch
+    e.profile_read(reset=True)
+    e.profile_enable(True, stride=1)
+    e.step_taylor(min(args.steps, 20), 0.005, 1.0, order, 4)
+    torch.cuda.synchronize()
     prof = e.profile_read(reset=True)
+    e.profile_enable(False)
     peak, peak_kind = load_peaks()
     t_ms, t_n = prof["taylor"]
     achieved = 40 * n ** 3 / (t_ms / t_n * 1e-3) / 1e9

@@ -96,6 +96,12 @@ const char* wfs_last_error(const wfs_handle* h);
  * pass whose bounded wait for a tile copy gave up is reported here, by wfs_get_psi
  * and by the observation calls as WFS_ERR_TIMEOUT (the status is then cleared). */
 int wfs_synchronize(wfs_handle* h);
+/* Limit of a copy-staged pass's wait for a staged tile, in seconds (default 1; at most
+ * 60). A limit of zero makes every such wait give up at once: the pass then stops
+ * without storing, and the next wfs_synchronize reports WFS_ERR_TIMEOUT once. This is
+ * the test hook for the expiry path; it has no counterpart in the reference, whose
+ * transforms are library calls. */
+int wfs_set_copy_wait_limit(wfs_handle* h, double seconds);
 
 /* Potential construction (sources/sim_state.py:210-255). */
 int wfs_potential_clear(wfs_handle* h);                                   /* V.fill(0): sources/potential.py:510 */
@@ -240,9 +246,12 @@ int wfs_batch_launch_count(wfs_batch* b, int64_t* out);
  * allocating routine. Scratch is one fixed device array of
  * WFS_NOALLOC_SCRATCH_DOUBLES doubles (1 MiB per GPU, held until exit):
  * grids with ceil(nx*ny/8) * (nbox + (loc ? 7 : 0)) > WFS_NOALLOC_SCRATCH_DOUBLES - 16
- * are rejected with WFS_ERR_UNSUPPORTED. The first call on a device looks up
- * the array's address (make it before any stream capture). Calls share the
- * array: calls that overlap on the GPU race. Message: wfs_global_error().
+ * are rejected with WFS_ERR_UNSUPPORTED. The first call in each CUDA context
+ * (once per device for runtime-API callers) looks up the array's address and
+ * caches it under the context's unique ID, so a context created after
+ * cudaDeviceReset or a non-primary context gets its own lookup; make that
+ * first call before any stream capture. Calls share the array: calls that
+ * overlap on the GPU race. Message: wfs_global_error().
  * ---------------------------------------------------------------------- */
 #define WFS_NOALLOC_SCRATCH_DOUBLES 131072
 int wfs_observe_noalloc(const void* psi_device, int32_t dtype, const int32_t n[3], const double extent[3],

@@ -52,3 +52,38 @@ def test_staged_pass_bit_identical_to_cp_async(n, tmp_path):
     assert a.dtype == np.complex64 and a.shape == n
     assert np.isfinite(a).all()
     assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_expired_tile_wait_reports_timeout_once_and_recovers():
+    """The expiry path of the copy-staged pass, made to run without any fault: a wait
+    limit of zero makes every tile wait give up at once. The pass must return (each CTA
+    stops after its first tile and drains its two copies in flight), the next
+    synchronisation must report WFS_ERR_TIMEOUT exactly once, and with the default limit
+    restored the engine must step correctly again."""
+    import time
+
+    from oracle import wfs_oracle as orc
+    from wavefunctionsimpython_gb300 import Engine
+    from wavefunctionsimpython_gb300._lib import WfsError
+
+    n, L = (64, 128, 128), (25.6, 51.2, 51.2)
+    e = Engine(n, L)
+    e.init_gaussian((3.0, 5.0, 5.0), (-3.0, 2.0, 0.0), (1.5, 0.5, 0.0))
+    psi0 = e.get_psi()
+    e.set_copy_wait_limit(0.0)
+    t0 = time.perf_counter()
+    e.step_split(1, 0.01, 1.0)
+    with pytest.raises(WfsError) as exc:
+        e.synchronize()
+    assert exc.value.code == 3  # WFS_ERR_TIMEOUT
+    assert time.perf_counter() - t0 < 30.0
+    e.synchronize()  # reported once: the status word was cleared
+    e.set_copy_wait_limit(1.0)
+    e.set_psi(psi0)
+    e.step_split(3, 0.01, 1.0)
+    e.synchronize()
+    dx = orc.delta_x(L, n)
+    ref = orc.split_step(psi0.astype(np.complex128), np.zeros(n, np.complex64), dx, 0.01, 1.0, nsteps=3)
+    got = e.get_psi()
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+    e.close()

@@ -9,7 +9,9 @@ its scratch in a fixed device array inside the library.
 
 These tests call it through the C ABI and compare it with wfs_observe (the
 handle-based entry point, which allocates its scratch) on two calls in a row,
-and check that a grid too large for the fixed scratch is refused.
+with the expected location alone, on a grid that needs exactly as many partial
+sums as the fixed scratch holds (also against the oracle's Simpson sums), and
+check that one more row of blocks, or a grid far too large, is refused.
 """
 import ctypes as C
 
@@ -89,3 +91,67 @@ def test_noalloc_rejects_grid_beyond_scratch():
                out.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert rc == WFS_ERR_UNSUPPORTED
     assert b"scratch" in lib.wfs_global_error()
+
+
+def test_noalloc_location_only_and_exact_scratch_limit():
+    """nbox = 0 with a location box (7 quantities), then a (16, 8191, 2) grid with one box
+    and a location box: ceil(16 * 8191 / 8) * 8 = 131056 partial sums, exactly what the
+    fixed scratch holds (accepted, checked against wfs_observe and the FP64 oracle); a
+    (16, 8192, 2) grid needs 131072 and is refused before anything is launched."""
+    import torch
+
+    from oracle import wfs_oracle as orc
+    from wavefunctionsimpython_gb300 import Engine
+    from wavefunctionsimpython_gb300._lib import WFS_C64, WFS_ERR_UNSUPPORTED, WFS_OK, load
+
+    lib = load()
+    stream = torch.cuda.Stream()
+    out = torch.full((16,), float("nan"), dtype=torch.float64, device="cuda")
+
+    # location only
+    n, L = (40, 24, 32), (20.0, 12.0, 16.0)
+    e = Engine(n, L, stream=stream.cuda_stream)
+    e.init_gaussian((2.0, 1.5, 2.0), (-2.0, 1.0, 0.5), (1.0, 0.0, 0.5))
+    loc = ((1, 2, 3), (37, 19, 27))
+    torch.cuda.synchronize()
+    rc = _call(lib, e.psi_device_ptr(), WFS_C64, n, L, [], loc, out.data_ptr(), stream.cuda_stream)
+    assert rc == WFS_OK, lib.wfs_global_error().decode()
+    stream.synchronize()
+    got = out.cpu().numpy()
+    _, er, er2 = e.observe([], loc)
+    np.testing.assert_allclose(got[0:3], er, rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(got[3:6], er2, rtol=1e-12, atol=0)
+    e.close()
+
+    # exactly at the limit
+    n, L = (16, 8191, 2), (8.0, 4095.5, 1.0)
+    e = Engine(n, L, stream=stream.cuda_stream)
+    rng = np.random.default_rng(11)
+    psi = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    e.set_psi(psi)
+    boxes = [((1, 10, 0), (13, 8001, 1))]
+    loc = ((0, 0, 0), (15, 8191, 1))
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        out.fill_(float("nan"))
+    rc = _call(lib, e.psi_device_ptr(), WFS_C64, n, L, boxes, loc, out.data_ptr(), stream.cuda_stream)
+    assert rc == WFS_OK, lib.wfs_global_error().decode()
+    stream.synchronize()
+    got = out.cpu().numpy()
+    probs, er, er2 = e.observe(boxes, loc)
+    np.testing.assert_allclose(got[:1], probs, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(got[1:4], er, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(got[4:7], er2, rtol=1e-12, atol=0)
+    dx = orc.delta_x(L, n)
+    np.testing.assert_allclose(got[0], orc.volume_probability(psi, dx, *boxes[0]), rtol=1e-6)
+    oer, oer2 = orc.expected_location(psi, dx, *loc)
+    np.testing.assert_allclose(got[1:4], oer, rtol=1e-5, atol=1e-6 * float(np.max(np.abs(oer2))) ** 0.5)
+    np.testing.assert_allclose(got[4:7], oer2, rtol=1e-6)
+    e.close()
+
+    # one block row more than the scratch holds
+    dummy = torch.zeros(8, dtype=torch.complex64, device="cuda")
+    rc = _call(lib, dummy.data_ptr(), WFS_C64, (16, 8192, 2), (8.0, 4096.0, 1.0), boxes, loc, out.data_ptr(),
+               stream.cuda_stream)
+    assert rc == WFS_ERR_UNSUPPORTED
+    assert b"131072" in lib.wfs_global_error()

@@ -29,6 +29,7 @@ MAX_BOX = 8
 # Every entry point include/wfs.h declares (checked by the CPU test suite).
 EXPORTED = [
     "wfs_abi_version", "wfs_global_error", "wfs_create", "wfs_destroy", "wfs_last_error", "wfs_synchronize",
+    "wfs_set_copy_wait_limit",
     "wfs_potential_clear", "wfs_potential_add_wall", "wfs_potential_add_absorbing", "wfs_potential_add_raw",
     "wfs_set_potential", "wfs_get_potential", "wfs_init_gaussian", "wfs_set_psi", "wfs_get_psi",
     "wfs_psi_device_ptr", "wfs_step_split", "wfs_step_taylor", "wfs_kinetic_operator", "wfs_potential_operator",
@@ -127,6 +128,7 @@ def load(path: str | os.PathLike | None = None):
         "wfs_destroy": ([vp], C.c_int),
         "wfs_last_error": ([vp], C.c_char_p),
         "wfs_synchronize": ([vp], C.c_int),
+        "wfs_set_copy_wait_limit": ([vp, dbl], C.c_int),
         "wfs_potential_clear": ([vp], C.c_int),
         "wfs_potential_add_wall": ([vp, C.POINTER(WallDesc)], C.c_int),
         "wfs_potential_add_absorbing": ([vp, C.POINTER(AbsorbingDesc)], C.c_int),
@@ -336,6 +338,10 @@ class Engine:
 
     def synchronize(self):
         self._ck(self.lib.wfs_synchronize(self.h))
+
+    def set_copy_wait_limit(self, seconds):
+        """Limit of a copy-staged pass's wait for a staged tile (test hook: 0 gives up at once)."""
+        self._ck(self.lib.wfs_set_copy_wait_limit(self.h, float(seconds)))
 
     # --- observables ---
     @staticmethod

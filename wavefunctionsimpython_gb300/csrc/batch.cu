@@ -20,6 +20,7 @@
 
 #include "../../include/wfs.h"
 #include "host_helpers.h"
+#include "per_device.h"
 #include "plane_kernels.cuh"
 
 using namespace wfs;
@@ -259,13 +260,14 @@ cudaError_t launch_batch(wfs_batch* b, int prog, int cluster, int swap) {
 }
 
 int set_kernel_attrs() {
-    static bool done = false;
-    if (done) return 0;
+    static PerDevice done;
+    const int dev = current_device();
+    if (done.get(dev)) return 0;
     for (auto k : {batch_kernel<false>, batch_kernel<true>}) {
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBatchSmem)) != cudaSuccess) return 1;
         if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 1;
     }
-    done = true;
+    done.put(dev, 1);
     return 0;
 }
 

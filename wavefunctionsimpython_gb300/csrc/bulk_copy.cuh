@@ -46,12 +46,17 @@ __device__ __forceinline__ uint64_t global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
     return t;
 }
-// Waits for the phase with the given parity to complete, for at most about one second.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+// Default limit of a bounded wait: about one second of global time.
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+// Waits for the phase with the given parity to complete, for at most limit_ns of global
+// time. A limit of 1 ns or less gives up at once without polling, which is how the
+// engine's test hook (wfs_set_copy_wait_limit) makes the expiry path run.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
+    if (limit_ns <= 1) return false;
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     while (!mbar_try_wait(bar, parity))
-        if (global_ns() - t0 > 1000000000ull) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     return true;
 }
 // Orders this thread's earlier generic-proxy accesses of shared memory before later

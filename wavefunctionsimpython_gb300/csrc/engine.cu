@@ -72,6 +72,7 @@ struct wfs_handle {
     double* dres;         // device results
     double* hres;         // pinned host results
     int* dflag;
+    uint64_t copy_wait_ns;  // limit of a copy-staged pass's wait for a tile (wfs_set_copy_wait_limit)
     std::string err;
     // per-pass CUDA-event profile (wfs_profile_enable / wfs_profile_read)
     bool prof_on;
@@ -216,6 +217,7 @@ PassArgs<R> base_args(wfs_handle* h, int axis) {
     a.tw = reinterpret_cast<const Cx<R>*>(h->tw[axis]);
     a.scale = R(1);
     a.status = h->dflag + 1;
+    a.wait_ns = h->copy_wait_ns;
     return a;
 }
 
@@ -595,6 +597,7 @@ int wfs_create(const wfs_grid_desc* d, wfs_handle** out) {
     h->rep = REP_REAL;
     h->prof_on = false;
     h->prof_stride = 1;
+    h->copy_wait_ns = kWaitLimitNs;
     h->steps_done = 0;
     h->launches = 0;
     h->schedule = WFS_SCHEDULE_AUTO;
@@ -677,6 +680,14 @@ int wfs_synchronize(wfs_handle* h) {
     CK(queue_status(h));
     CK(cudaStreamSynchronize(h->stream));
     return take_status(h);
+}
+
+int wfs_set_copy_wait_limit(wfs_handle* h, double seconds) {
+    if (!h) return dispatch_err(h);
+    if (!(seconds >= 0.0) || seconds > 60.0) return set_err(h, WFS_ERR_ARG, "wait limit must lie in [0, 60] seconds");
+    const double ns = seconds * 1e9;
+    h->copy_wait_ns = ns <= 1.0 ? 1 : uint64_t(ns);
+    return WFS_OK;
 }
 
 int wfs_potential_clear(wfs_handle* h) {

@@ -3,6 +3,7 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "fft_kernels.cuh"
 
@@ -23,6 +24,49 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
         return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
     }();
     return fn;
+}
+
+// Encoded tensor maps of recent launches. A map describes psi's address, shape and
+// strides; the split step launches the x pass on the same psi every step, so the
+// encoding (a host call of a few microseconds) is done once per array instead of
+// once per launch. Keyed by device, address, shape, strides and tile width.
+struct MapKey {
+    int dev;
+    const void* data;
+    int64_t ncols, rows, outer, row_stride, outer_stride;
+    int width;
+    bool operator==(const MapKey& o) const {
+        return dev == o.dev && data == o.data && ncols == o.ncols && rows == o.rows && outer == o.outer &&
+               row_stride == o.row_stride && outer_stride == o.outer_stride && width == o.width;
+    }
+};
+struct MapCache {
+    static constexpr int kSlots = 8;
+    std::mutex mu;
+    MapKey key[kSlots];
+    CUtensorMap map[kSlots];
+    bool used[kSlots] = {};
+    int next = 0;
+};
+MapCache g_maps;
+
+bool cached_map(const MapKey& k, CUtensorMap* out) {
+    std::lock_guard<std::mutex> lk(g_maps.mu);
+    for (int i = 0; i < MapCache::kSlots; ++i)
+        if (g_maps.used[i] && g_maps.key[i] == k) {
+            *out = g_maps.map[i];
+            return true;
+        }
+    return false;
+}
+
+void store_map(const MapKey& k, const CUtensorMap& m) {
+    std::lock_guard<std::mutex> lk(g_maps.mu);
+    const int i = g_maps.next;
+    g_maps.key[i] = k;
+    g_maps.map[i] = m;
+    g_maps.used[i] = true;
+    g_maps.next = (i + 1) % MapCache::kSlots;
 }
 
 // The copy-staged strided pass is the default where it applies; WFS_STRIDED_STAGED=0 in the
@@ -59,17 +103,23 @@ cudaError_t run_strided_staged(const PassArgs<float>& a0, int64_t outer_count, c
         const cuuint32_t estr[3] = {1, 1, 1};
         if ((strides[0] % 16) || (strides[1] % 16) || a0.row_stride < a0.ncols || zs < int64_t(L) * a0.row_stride)
             return cudaSuccess;
+        const int dev = current_device();
+        const MapKey key{dev, a0.data, int64_t(a0.ncols), int64_t(L), outer_count, int64_t(a0.row_stride), zs, W};
         CUtensorMap map;
-        if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, a0.data, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return cudaSuccess;
+        if (!cached_map(key, &map)) {
+            if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, a0.data, dims, strides, box, estr,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return cudaSuccess;
+            store_map(key, map);
+        }
         std::memcpy(&sa.map, &map, sizeof(map));
         // staging slots, two mbarriers, twiddle rows of both plans and the kinetic x factors
         const size_t smem = 128 + 2 * size_t(L) * W * sizeof(Cx<float>) + 2 * sizeof(uint64_t) +
                             3 * size_t(L) * sizeof(Cx<float>);
         auto kern = fft_strided_staged_kernel<P, Q, W, OP>;
-        static int blocks_per_sm = 0;
+        static PerDevice occupancy;
+        int blocks_per_sm = occupancy.get(dev);
         if (blocks_per_sm == 0) {
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if (e == cudaSuccess)  // WFS_MINB_STAGED blocks of two L x W tiles each need the largest carveout
@@ -80,6 +130,7 @@ cudaError_t run_strided_staged(const PassArgs<float>& a0, int64_t outer_count, c
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, T * W, smem);
             if (e != cudaSuccess) return e;
             blocks_per_sm = nb > 0 ? nb : 1;
+            occupancy.put(dev, blocks_per_sm);
         }
         const int64_t nitems = outer_count * tiles;
         const int64_t cap = int64_t(blocks_per_sm) * device_sm_count();

@@ -17,6 +17,8 @@
 // gives each CTA W whole rows.
 #pragma once
 
+#include "per_device.h"
+
 #include <cmath>
 #include <cstdlib>
 
@@ -305,9 +307,7 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_STAGED)
     const Cx<R>* tw_f = tsm;
     const Cx<R>* tw_i = tsm + L;
     const Cx<R>* k_row = tsm + 2 * L;
-    bool expired = false;
     auto issue = [&](int64_t item, int slot) {  // thread 0 only
-        if (expired) return;
         const uint32_t bar = smem_addr(&bars[slot]);
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(bar, uint32_t(L * W * sizeof(Cx<R>)));
@@ -322,10 +322,8 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_STAGED)
         const int slot = k & 1;
         const int64_t next = item + gridDim.x;
         if (tid == 0 && next < nitems) issue(next, slot ^ 1);
-        if (!mbar_wait_bounded(smem_addr(&bars[slot]), uint32_t((k >> 1) & 1))) {
-            if (!expired && a.status) atomicOr(a.status, 1);
-            expired = true;
-        }
+        const bool waited =
+            mbar_wait_bounded(smem_addr(&bars[slot]), uint32_t((k >> 1) & 1), a.wait_ns ? a.wait_ns : kWaitLimitNs);
         const int tile = int(item % a.tiles);
         const int64_t outer = item / a.tiles;
         const int col = tile * W + c;
@@ -341,7 +339,7 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_STAGED)
         if constexpr (OP == OP_PLAIN) {
             if (a.dir < 0) two_stage<P, Q, -1, TWM>(a1, a2, sm, tw_f, t, sidx_f);
             else two_stage<P, Q, +1, TWM>(a1, a2, sm, tw_f, t, sidx_f);
-            if (active && t < Q) {
+            if (waited && active && t < Q) {
 #pragma unroll
                 for (int kk = 0; kk < P; ++kk) base[(t + Q * kk) * rs] = scale(a2[kk], a.scale);
             }
@@ -355,17 +353,25 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_STAGED)
             }
             __syncthreads();
             two_stage<Q, P, +1, TWM>(a2, a1, sm, tw_i, t, sidx_i);
-            if (active && t < P) {
+            if (waited && active && t < P) {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) base[(t + P * i) * rs] = a1[i];
             }
         }
-        __syncthreads();  // this slot is refilled with the item after next
-    }
-    // after an expired wait a copy may still be landing: wait (bounded) before the CTA exits
-    if (tid == 0 && expired) {
-        if (k > 0) mbar_wait_bounded(smem_addr(&bars[(k - 1) & 1]), uint32_t(((k - 1) >> 1) & 1));
-        if (k > 1) mbar_wait_bounded(smem_addr(&bars[(k - 2) & 1]), uint32_t(((k - 2) >> 1) & 1));
+        // The barrier that lets this slot be refilled with the item after next also tells
+        // every thread whether any thread's wait for this tile ran out. If one did, the CTA
+        // reports it (the host reads the status word at its next synchronisation) and
+        // stops: the tiles it has not stored are left as they were, no further copies are
+        // issued, and thread 0 first waits, with the default bound, for the two copies that
+        // may still be landing in this CTA's shared memory (this tile's and the next one's).
+        if (__syncthreads_or(!waited)) {
+            if (tid == 0) {
+                if (a.status) atomicOr(a.status, 1);
+                mbar_wait_bounded(smem_addr(&bars[slot]), uint32_t((k >> 1) & 1));
+                if (next < nitems) mbar_wait_bounded(smem_addr(&bars[slot ^ 1]), uint32_t(((k + 1) >> 1) & 1));
+            }
+            return;
+        }
     }
 }
 
@@ -496,11 +502,15 @@ inline bool strided_pipeline_enabled() {
     return on != 0;
 }
 inline int device_sm_count() {
-    static int n = 0;
+    static PerDevice sms;
+    const int dev = current_device();
+    int n = sms.get(dev);
     if (n == 0) {
-        int dev = 0, v = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+        int v = 0;
+        if (dev >= 0 && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0) {
             n = v;
+            sms.put(dev, n);
+        }
     }
     return n > 0 ? n : 1;
 }
@@ -511,7 +521,9 @@ cudaError_t run_strided_pipe(const PassArgs<R>& a, int64_t outer_count, cudaStre
     constexpr int W = StridedW<R, T>::value;
     const size_t smem = 2 * size_t(L) * W * sizeof(Cx<R>);
     auto kern = fft_strided_pipe_kernel<R, P, Q, W, OP>;
-    static int blocks_per_sm = 0;
+    static PerDevice occupancy;
+    const int dev = current_device();
+    int blocks_per_sm = occupancy.get(dev);
     if (blocks_per_sm == 0) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
@@ -519,6 +531,7 @@ cudaError_t run_strided_pipe(const PassArgs<R>& a, int64_t outer_count, cudaStre
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, T * W, smem);
         if (e != cudaSuccess) return e;
         blocks_per_sm = nb > 0 ? nb : 1;
+        occupancy.put(dev, blocks_per_sm);
     }
     const int64_t nitems = outer_count * a.tiles;
     const int64_t cap = int64_t(blocks_per_sm) * device_sm_count();
@@ -539,11 +552,12 @@ cudaError_t run_strided(const PassArgs<R>& a0, int64_t outer_count, cudaStream_t
     }
     const size_t smem = size_t(L) * W * sizeof(Cx<R>);
     auto kern = fft_strided_kernel<R, P, Q, W, OP>;
-    static bool attr_set = false;
-    if (!attr_set) {
+    static PerDevice attr_set;
+    const int dev = current_device();
+    if (!attr_set.get(dev)) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        attr_set.put(dev, 1);
     }
     const int64_t grid = outer_count * a.tiles;
     kern<<<dim3(unsigned(grid)), dim3(T * W), smem, s>>>(a);
@@ -558,11 +572,12 @@ cudaError_t run_contig(const PassArgs<R>& a, cudaStream_t s, int* grid_out) {
     size_t smem = size_t(W) * RS * sizeof(Cx<R>);
     if (OP == OP_OBS) smem = smem > (kMaxBox + kLocQ) * 32 * sizeof(double) ? smem : (kMaxBox + kLocQ) * 32 * sizeof(double);
     auto kern = fft_contig_kernel<R, P, Q, W, OP>;
-    static bool attr_set = false;
-    if (!attr_set) {
+    static PerDevice attr_set;
+    const int dev = current_device();
+    if (!attr_set.get(dev)) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        attr_set.put(dev, 1);
     }
     const int64_t grid = (a.nrows + W - 1) / W;
     if (grid_out) *grid_out = int(grid);

@@ -403,10 +403,8 @@ template cudaError_t launch_mul_inplace<double>(Cx<double>*, const Cx<double>*, 
 // ---------------------------------------------------------------------------
 // Observables on real-space psi: one warp per (x, y) row, per-CTA FP64 partials.
 // ---------------------------------------------------------------------------
-constexpr int kObsRowsPerCta = 8;
-
 template <typename R>
-__global__ void __launch_bounds__(256) observe_real_kernel(const Cx<R>* __restrict__ psi, const ObsArgs o) {
+__global__ void __launch_bounds__(32 * kObsRowsPerCta) observe_real_kernel(const Cx<R>* __restrict__ psi, const ObsArgs o) {
     __shared__ double scratch[(kMaxBox + kLocQ) * 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t nrows = int64_t(o.n[0]) * o.n[1];

@@ -30,6 +30,7 @@
 #include "../../include/wfs.h"
 #include "../../include/wfs_fno.h"
 #include "host_helpers.h"
+#include "per_device.h"
 #include "kernels.h"
 
 namespace wfs {
@@ -655,11 +656,12 @@ int wfs_fno_weight_grad(const void* g, int32_t cout, const void* x, int32_t cin,
     const int64_t ntiles = (int64_t(B) * n3 + kWgTile - 1) / kWgTile;
     const int nblocks = int(ntiles < kWgBlocks ? ntiles : kWgBlocks);
     const size_t smem = size_t(cout + cin + 1) * (kWgTile + 1) * sizeof(float);
-    static bool attr = false;
-    if (!attr) {
+    static PerDevice attr;
+    const int dev = current_device();
+    if (!attr.get(dev)) {
         if (cudaFuncSetAttribute(wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 80 * 1024) != cudaSuccess)
             return WFS_ERR_CUDA;
-        attr = true;
+        attr.put(dev, 1);
     }
     wgrad_kernel<<<nblocks, 256, smem, s>>>((const float2*)g, cout, (const float2*)x, cin, B, n3, partials);
     const int nq = cout * (cin + 1);

@@ -47,6 +47,7 @@ inline bool plan_pq(int L, int& P, int& Q) {
 
 constexpr int kMaxBox = 8;      // volume-probability boxes per fused observation
 constexpr int kLocQ = 7;        // location box sums: S, Sx, Sy, Sz, Sxx, Syy, Szz
+constexpr int kObsRowsPerCta = 8;  // (x, y) rows per CTA of observe_real_kernel: one warp per row
 
 enum PassOp { OP_PLAIN = 0, OP_KIN = 1, OP_VPH = 2, OP_OBS = 3 };
 
@@ -91,6 +92,7 @@ struct PassArgs {
     // OP_OBS (contiguous, read-only): observe scale * F^-1(x); rows are (x, y) = (q / ny, q % ny)
     ObsArgs obs;
     int* status;            // copy-staged passes: bit 0 set when a bounded wait gave up (may be null)
+    uint64_t wait_ns;       // copy-staged passes: limit of the wait for a staged tile (0: the default, 1: give up at once)
 };
 
 template <typename R>

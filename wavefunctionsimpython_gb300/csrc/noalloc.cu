@@ -12,10 +12,14 @@
 // The reduction needs scratch for its per-block partial sums. Here it lives in
 // one file-scope __device__ array of fixed size (kNoAllocScratchDoubles
 // doubles, 1 MiB); every GPU that loads this library keeps it until the
-// process exits. Its device address is looked up once per device with
-// cudaGetSymbolAddress (host code must not use the symbol's name as an
-// address) on the first call made on that device; make that first call
-// before capturing any stream into a CUDA graph.
+// process exits. Its device address is looked up with cudaGetSymbolAddress
+// (host code must not use the symbol's name as an address) on the first call
+// made in each CUDA context, i.e. once per device for callers of the runtime
+// API, and cached under that context's unique ID; make that first call before
+// capturing any stream into a CUDA graph. Because the ID is unique for the
+// life of the process, a context created after cudaDeviceReset, or a
+// non-primary context the caller made current, gets its own lookup instead of
+// a stale address.
 //
 // All calls on a device share the one array and it keeps what the last call
 // left in it. Every slot a call reads is written earlier in the same call
@@ -33,7 +37,6 @@ namespace wfs {
 
 constexpr int kNoAllocScratchDoubles = WFS_NOALLOC_SCRATCH_DOUBLES;
 constexpr int kNoAllocRawSlot = kNoAllocScratchDoubles - 16;   // 16 doubles for the block-reduced sums
-constexpr int kNoAllocRowsPerCta = 8;                          // rows per block of the reduction kernel
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
@@ -50,8 +53,38 @@ __global__ void noalloc_finish_kernel(const double* __restrict__ raw, int nbox, 
 
 namespace {
 
+// Scratch addresses by CUDA context: cuCtxGetCurrent and cuCtxGetId reached through the
+// runtime's driver entry points (no link-time libcuda dependency).
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+template <typename F>
+F driver_fn(const char* name, int version) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, version, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+        p = nullptr;
+    return reinterpret_cast<F>(p);
+}
+
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    double* ptr;
+};
+constexpr int kScratchSlots = 64;
 std::mutex g_noalloc_mutex;
-double* g_noalloc_ptr[64] = {nullptr};
+ScratchSlot g_noalloc_slot[kScratchSlots] = {};
+int g_noalloc_next = 0;
+
+// The current context's unique ID; 0 when it cannot be read (then nothing is cached).
+unsigned long long current_context_id() {
+    static const CtxGetCurrentFn get_current = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent", 4000);
+    static const CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId", 12000);
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -96,31 +129,41 @@ extern "C" int wfs_observe_noalloc(const void* psi_device, int32_t dtype, const 
     o.has_loc = loc ? 1 : 0;
     if (loc && !cp(*loc, o.loc)) return fail(WFS_ERR_ARG, "location box outside the grid");
     o.nq = nbox + (loc ? kLocQ : 0);
-    // the reduction uses one block per 8 (x, y) rows and nq partial sums per block
+    // the reduction (launch_observe_real) uses one block per kObsRowsPerCta (x, y) rows and
+    // nq partial sums per block
     const int64_t rows = int64_t(n[0]) * n[1];
-    const int64_t blocks = (rows + kNoAllocRowsPerCta - 1) / kNoAllocRowsPerCta;
+    const int64_t blocks = (rows + kObsRowsPerCta - 1) / kObsRowsPerCta;
     if (blocks * o.nq > kNoAllocRawSlot)
         return fail(WFS_ERR_UNSUPPORTED,
-                    "grid too large for the fixed scratch: ceil(nx*ny/8) * (quantities) must be <= " +
-                        std::to_string(kNoAllocRawSlot) + ", got " + std::to_string(blocks * o.nq));
+                    "grid too large for the fixed scratch: ceil(nx*ny/" + std::to_string(kObsRowsPerCta) +
+                        ") * (quantities) must be <= " + std::to_string(kNoAllocRawSlot) + ", got " +
+                        std::to_string(blocks * o.nq));
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(WFS_ERR_CUDA, "no current CUDA device");
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(WFS_ERR_CUDA, "no current CUDA device");
     double* scratch = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_noalloc_mutex);
-        if (!g_noalloc_ptr[dev]) {
+        const unsigned long long id = current_context_id();
+        for (int i = 0; id && i < kScratchSlots && !scratch; ++i)
+            if (g_noalloc_slot[i].ctx_id == id) scratch = g_noalloc_slot[i].ptr;
+        if (!scratch) {
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess || !p)
                 return fail(WFS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_noalloc_ptr[dev] = static_cast<double*>(p);
+            scratch = static_cast<double*>(p);
+            if (id) {
+                g_noalloc_slot[g_noalloc_next] = {id, scratch};
+                g_noalloc_next = (g_noalloc_next + 1) % kScratchSlots;
+            }
         }
-        scratch = g_noalloc_ptr[dev];
     }
     o.partials = scratch;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     int grid = 0;
-    cudaError_t e = (dtype == WFS_C64)
+    cudaError_t e = cudaSuccess;
+    if (blocks > INT32_MAX) return fail(WFS_ERR_UNSUPPORTED, "grid too large");
+    e = (dtype == WFS_C64)
                         ? launch_observe_real<float>(reinterpret_cast<const Cx<float>*>(psi_device), o, s, &grid)
                         : launch_observe_real<double>(reinterpret_cast<const Cx<double>*>(psi_device), o, s, &grid);
     if (e == cudaSuccess) e = launch_reduce_partials(scratch, grid, o.nq, scratch + kNoAllocRawSlot, s);

@@ -217,15 +217,16 @@ cudaError_t run_plane(const PlaneArgs<R>& a, int64_t nplanes, cudaStream_t s) {
     constexpr int RSZ = cmax(QZ * (PZ + 1), PZ * (QZ + 1));
     const size_t smem = sizeof(Cx<R>) * (size_t(cmax(LY * WY, WZ * RSZ)) + (TSM ? size_t(PY * QY + LZ) : 0));
     auto kern = plane_step_kernel<R, LY, LZ, CL, NT, TSM>;
-    static bool attr_set = false;
-    if (!attr_set) {
+    static PerDevice attr_set;
+    const int dev = current_device();
+    if (!attr_set.get(dev)) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
         if (CL > 8) {
             e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
             if (e != cudaSuccess) return e;
         }
-        attr_set = true;
+        attr_set.put(dev, 1);
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(nplanes * CL));
