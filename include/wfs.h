@@ -108,6 +108,18 @@ int wfs_potential_clear(wfs_handle* h);                                   /* V.f
 int wfs_potential_add_wall(wfs_handle* h, const wfs_wall* w);              /* PotentialWall.add_potential: sources/potential.py:201-242 */
 int wfs_potential_add_absorbing(wfs_handle* h, const wfs_absorbing* a);    /* AbsorbingBoundaryCondition.add_potential: sources/potential.py:108-158 */
 int wfs_potential_add_raw(wfs_handle* h, const void* data, int32_t raw_type, int32_t on_device); /* PreInitializedPotential.add_potential: sources/potential.py:47-55 */
+/* Dynamic potential mode: SimState.update_potential (sources/sim_state.py:466-509) with
+ * generate_potential_from_walls_and_drain (sources/potential.py:508-522). After every
+ * later step (split or power series) each wall's centre moves by velocity * dt (3 values
+ * per wall, Bohr per hbar/Hartree) with its x clamped at 0, and V becomes the walls plus
+ * the absorbing ramp (NULL: none). The first update rebuilds V whole, dropping any
+ * pre-initialised potential as the reference's rebuild does; later updates rewrite only
+ * the voxels a moving wall covered before or covers after the move (V and the phase
+ * table), so the step loop stays on the device. nwall = 0 ends the mode; at most 8 walls. */
+int wfs_set_dynamic_walls(wfs_handle* h, const wfs_wall* walls, const double* velocity, int32_t nwall,
+                          const wfs_absorbing* absorbing);
+/* Current centres of the dynamic walls, 3 per wall (nwall must equal the number set). */
+int wfs_get_dynamic_walls(wfs_handle* h, double* centers, int32_t nwall);
 int wfs_set_potential(wfs_handle* h, const void* v_c64, int32_t on_device);
 int wfs_get_potential(wfs_handle* h, void* v_c64, int32_t to_device);
 

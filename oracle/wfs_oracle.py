@@ -210,6 +210,16 @@ def wall_frame(normal, slit_rotation_radian):
     up.x = 0 and up.z = 1); right = normalize(cross(n, up)) rotated by
     slit_rotation_radian around n; cos/sin of the half angle are the float32
     roundings of the exact values.
+
+    The reference takes cosf/sinf on the device, and those are not correctly
+    rounded at every argument: sinf(0.7853982f), the half angle of a pi/2 slit
+    rotation, is 0.70710683 on the device against 0.70710677 correctly rounded.
+    Such a one-ulp difference moves a slit edge by about 1e-7 Bohr, which changes
+    only voxels that lie exactly on the edge in float32 arithmetic (a slit edge at
+    |y| = 1 on a grid of spacing 0.5, for example). The engine calls the device
+    functions and matches the reference's own kernels there
+    (tests/test_gpu_refpath.py); tests against this oracle use geometries
+    without such ties.
     """
     n = np.asarray(normal, dtype=np.float64)
     n = (n / math.sqrt(float(np.dot(n, n)))).astype(np.float32)  # sources/potential.py:180
@@ -568,6 +578,42 @@ def split_step(psi, V, dx, dt, mass, nsteps=1, double_precision=None, fft=None):
         psi *= K
         psi = ifftn(psi, norm="ortho").astype(C, copy=False)
     return psi
+
+
+def advect_walls(walls, velocities, dt):
+    """One update of the moving walls (sources/sim_state.py:470-473): centre += v dt in
+    float64, then the x centre is clamped at 0. Returns new Wall objects."""
+    import dataclasses
+
+    out = []
+    for w, v in zip(walls, velocities):
+        c = np.asarray(w.center_bohr_radii_3, np.float64) + np.asarray(v, np.float64) * dt
+        if c[0] < 0.0:
+            c[0] = 0.0
+        out.append(dataclasses.replace(w, center_bohr_radii_3=tuple(float(x) for x in c)))
+    return out
+
+
+def rebuild_potential(n, dx, walls, absorbing):
+    """generate_potential_from_walls_and_drain (sources/potential.py:508-522): V.fill(0),
+    every wall added, then the absorbing ramp."""
+    V = np.zeros(n, np.complex64)
+    for w in walls:
+        add_potential_wall(V, dx, w)
+    if absorbing is not None:
+        add_absorbing_potential(V, dx, absorbing)
+    return V
+
+
+def dynamic_split_run(psi, V, dx, dt, mass, walls, velocities, absorbing, nsteps):
+    """The reference's loop in dynamic potential mode (sources/core_sim.py:19-23):
+    evolve one split step with the current V, then advect the walls and rebuild V.
+    FP64 propagation; returns (psi, V, walls)."""
+    for _ in range(nsteps):
+        psi = split_step(psi, V, dx, dt, mass, nsteps=1, double_precision=True)
+        walls = advect_walls(walls, velocities, dt)
+        V = rebuild_potential(V.shape, dx, walls, absorbing)
+    return psi, V, walls
 
 
 # ---------------------------------------------------------------------------

@@ -173,3 +173,49 @@ def test_checkpoint_resume_is_exact_with_moving_wall(tmp_path, method):
     c.set_use_cache(False)
     with pytest.raises(ValueError):
         c.load_checkpoint(ckpt)
+
+
+def test_run_iteration_moving_wall_stays_on_device(tmp_path):
+    """Dynamic potential mode with a moving wall: run_iteration keeps the fused device loop
+    (the engine advects the wall and rebuilds V after each step) and records the same
+    series as the reference's measure / evolve / update_potential loop, restated by the
+    oracle with the engine's absorbing ramp (which does not move; the ramp's float32 atan
+    and pow round differently on the host by up to two ulps)."""
+    from wavefunctionsimpython_gb300 import config_read_helper, core_sim
+    from wavefunctionsimpython_gb300.iter_data import IterData
+    from wavefunctionsimpython_gb300.measurement import MeasurementTools
+    from wavefunctionsimpython_gb300.sim_state import SimState
+
+    config_read_helper.QUIET = True
+    cfg = base_config(tmp_path)
+    cfg["simulation"]["is_dynamic_potential_mode"] = True
+    w = cfg["potential"]["walls"][0]
+    w["velocity_bohr_radius_hartree_per_h_bar_3"] = [-0.8, 0.3, 0.0]
+    w["slope_exponent"] = 1.0  # a linear slope: the host's float32 pow and the device's powf agree
+    s = SimState(copy.deepcopy(cfg))
+    s.set_use_cache(False)
+    s.initialize_state()
+    mt = MeasurementTools(copy.deepcopy(cfg), s)
+    it = IterData(cfg)
+    assert core_sim._can_fuse(s, mt)
+    dx, V, psi = oracle_run(cfg, s)
+    ramp = s.engine.get_potential().imag.astype(np.float32)
+    wall = orc.Wall(potential_hartree=w["potential_hartree"], center_bohr_radii_3=tuple(w["center_bohr_radii_3"]),
+                    normal_vector_3=tuple(w["normal_vector_3"]), plateau_thickness_bohr_radii=w["plateau_thickness_bohr_radii"],
+                    slope_thickness_bohr_radii=w["slope_thickness_bohr_radii"], slope_exponent=w["slope_exponent"],
+                    slit_count=w["slit_count"], slit_spacing_bohr_radii=w["slit_spacing_bohr_radii"],
+                    slit_width_bohr_radii=w["slit_width_bohr_radii"], slit_rotation_radian=w["slit_rotation_radian"])
+    walls, vel = [wall], [w["velocity_bohr_radius_hartree_per_h_bar_3"]]
+    V = (V.real + 1j * ramp).astype(np.complex64)
+    core_sim.run_iteration(s, mt, it)
+    dt = cfg["simulation"]["delta_time_h_bar_per_hartree"]
+    vols = mt.active_volume_probabilities()
+    for i in range(cfg["simulation"]["total_iteration_count"]):
+        for v in vols:
+            assert abs(v.get_probability_evolution_with_name()[0][i] - orc.volume_probability(psi, dx, *v.box)) < 1e-9
+        psi = orc.split_step(psi, V, dx, dt, 1.0, nsteps=1)
+        walls = orc.advect_walls(walls, vel, dt)
+        V = (orc.rebuild_potential(V.shape, dx, walls, None).real + 1j * ramp).astype(np.complex64)
+    assert np.array_equal(s.engine.get_potential(), V)
+    np.testing.assert_array_equal(s.get_potential_walls()[0].center_bohr_radii_3, walls[0].center_bohr_radii_3)
+    assert np.linalg.norm(s.get_wave_function() - psi) / np.linalg.norm(psi) < 1e-11

@@ -146,3 +146,20 @@ def test_absorbing_ramp_zero_inside_box_and_negative_outside():
     d = -10.0 - r[i]   # -dB.x, with dB.x = r - bottom < 0
     expect = (d / (16.0 - 10.0)) ** 2 * -50.0
     assert U[i, 16, 16] == pytest.approx(expect, rel=1e-5)
+
+
+def test_dynamic_rebuild_matches_initial_build_and_clamps():
+    """generate_potential_from_walls_and_drain (walls, then the ramp, from zero) gives the
+    initial potential back when nothing moved, and advection clamps the x centre at 0."""
+    n, L = (16, 16, 16), (8.0, 8.0, 8.0)
+    dx = orc.delta_x(L, n)
+    walls = [orc.Wall(potential_hartree=3.0, center_bohr_radii_3=(0.1, 0.0, 0.0), plateau_thickness_bohr_radii=1.0,
+                      slope_thickness_bohr_radii=0.5, slit_count=1, slit_width_bohr_radii=1.0)]
+    ab = orc.Absorbing(bottom=(-3.0,) * 3, top=(3.0,) * 3, offset=0.2, potential_pos=(-10.0,) * 3,
+                       potential_neg=(-10.0,) * 3, exponent_pos=(2.0,) * 3, exponent_neg=(2.0,) * 3)
+    sc = orc.Scenario(n=n, extent=L, sigma=(1.0,) * 3, r0=(0.0,) * 3, k0=(0.0,) * 3, dt=0.02, walls=walls,
+                      absorbing=ab)
+    assert np.array_equal(orc.rebuild_potential(n, dx, walls, ab), sc.potential())
+    moved = orc.advect_walls(walls, [(-3.0, 1.0, 0.0)], 0.05)
+    assert moved[0].center_bohr_radii_3 == (0.0, 0.05, 0.0)
+    assert not np.array_equal(orc.rebuild_potential(n, dx, moved, ab), sc.potential())

@@ -31,7 +31,7 @@ EXPORTED = [
     "wfs_abi_version", "wfs_global_error", "wfs_create", "wfs_destroy", "wfs_last_error", "wfs_synchronize",
     "wfs_set_copy_wait_limit",
     "wfs_potential_clear", "wfs_potential_add_wall", "wfs_potential_add_absorbing", "wfs_potential_add_raw",
-    "wfs_set_potential", "wfs_get_potential", "wfs_init_gaussian", "wfs_set_psi", "wfs_get_psi",
+    "wfs_set_potential", "wfs_get_potential", "wfs_set_dynamic_walls", "wfs_get_dynamic_walls", "wfs_init_gaussian", "wfs_set_psi", "wfs_get_psi",
     "wfs_psi_device_ptr", "wfs_step_split", "wfs_step_taylor", "wfs_kinetic_operator", "wfs_potential_operator",
     "wfs_observe", "wfs_run_split", "wfs_norm", "wfs_profile_enable", "wfs_profile_read", "wfs_launch_count",
     "wfs_set_schedule", "wfs_split_step_gain",
@@ -132,6 +132,8 @@ def load(path: str | os.PathLike | None = None):
         "wfs_potential_clear": ([vp], C.c_int),
         "wfs_potential_add_wall": ([vp, C.POINTER(WallDesc)], C.c_int),
         "wfs_potential_add_absorbing": ([vp, C.POINTER(AbsorbingDesc)], C.c_int),
+        "wfs_set_dynamic_walls": ([vp, C.POINTER(WallDesc), dp, i32, C.POINTER(AbsorbingDesc)], C.c_int),
+        "wfs_get_dynamic_walls": ([vp, dp, i32], C.c_int),
         "wfs_potential_add_raw": ([vp, vp, i32, i32], C.c_int),
         "wfs_set_potential": ([vp, vp, i32], C.c_int),
         "wfs_get_potential": ([vp, vp, i32], C.c_int),
@@ -264,6 +266,35 @@ class Engine:
         a = AbsorbingDesc(_d3(bottom), _d3(top), float(offset), _d3(potential_pos), _d3(potential_neg),
                           _d3(exponent_pos), _d3(exponent_neg))
         self._ck(self.lib.wfs_potential_add_absorbing(self.h, C.byref(a)))
+
+    def set_dynamic_walls(self, walls, velocities, absorbing=None):
+        """Dynamic potential mode. walls: sequences of add_wall's arguments (potential,
+        center, normal, plateau, slope, slope_exponent, slit_count, slit_spacing,
+        slit_width, slit_rotation); velocities: one 3-vector per wall; absorbing: the
+        seven add_absorbing arguments or None. After every later step the walls advect
+        and V is rebuilt from them and the absorbing ramp on the device."""
+        n = len(walls)
+        arr = (WallDesc * max(n, 1))()
+        for i, w in enumerate(walls):
+            defaults = [0.0, 1.0, 0, 1.0, 0.5, 0.0]  # slope, slope exponent, slits, spacing, width, rotation
+            w = list(w) + defaults[len(w) - 4:]
+            arr[i] = WallDesc(float(w[0]), _d3(w[1]), _d3(w[2]), float(w[3]), float(w[4]), float(w[5]), int(w[6]),
+                              float(w[7]), float(w[8]), float(w[9]))
+        vel = np.ascontiguousarray(np.asarray(velocities, np.float64).reshape(n, 3) if n else np.zeros((1, 3)))
+        ab = None
+        if absorbing is not None:
+            b, t, off, pp, pn, ep, en = absorbing
+            ab = AbsorbingDesc(_d3(b), _d3(t), float(off), _d3(pp), _d3(pn), _d3(ep), _d3(en))
+        self._ck(self.lib.wfs_set_dynamic_walls(self.h, arr, vel.ctypes.data_as(C.POINTER(C.c_double)), n,
+                                                C.byref(ab) if ab is not None else None))
+        self._ndyn = n
+
+    def get_dynamic_walls(self):
+        """Current centres of the dynamic walls, shape (nwall, 3)."""
+        n = getattr(self, "_ndyn", 0)
+        out = np.zeros((max(n, 1), 3), np.float64)
+        self._ck(self.lib.wfs_get_dynamic_walls(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), n))
+        return out[:n]
 
     def add_raw_potential(self, array: np.ndarray):
         arr = np.ascontiguousarray(array)

@@ -3,9 +3,10 @@
 ``time_step`` keeps the reference order (measure, evolve, update potential).
 ``run_iteration`` runs the whole loop on the device when every enabled
 measurement is a fused observable (volume probabilities and the expected
-location), no wave function is saved and no wall moves: the engine then
-records the observables before each step, exactly as the per-step loop
-would, without a host round trip per step. Otherwise it steps from Python.
+location) and no wave function is saved: the engine then records the
+observables before each step, exactly as the per-step loop would, and in
+dynamic potential mode advects the walls and rebuilds V after each step,
+without a host round trip per step. Otherwise it steps from Python.
 The loop stops between chunks on SIGINT and calls ``finish`` (the reference's
 ``write_snapshot`` + ``finish`` + exit, sources/core_sim.py:52-55).
 """
@@ -31,7 +32,7 @@ def time_step(sim_state: SimState, measurement_tools: MeasurementTools, iter_dat
 
 def _can_fuse(sim_state: SimState, mt: MeasurementTools) -> bool:
     return (sim_state.get_simulation_method() == SimulationMethod.FOURIER and mt.fusable()
-            and not sim_state.is_wave_function_saving() and not sim_state.has_moving_potential())
+            and not sim_state.is_wave_function_saving())
 
 
 def run_iteration(sim_state: SimState, measurement_tools: MeasurementTools, iter_data: IterData,
@@ -67,6 +68,7 @@ def run_iteration(sim_state: SimState, measurement_tools: MeasurementTools, iter
                     er = locs[k, :3] if loc is not None else None
                     er2 = locs[k, 3:] if loc is not None else None
                     measurement_tools.record(probs[k] if boxes else [], er, er2)
+                sim_state.sync_dynamic_walls()
                 i += n
                 iter_data.i = i
         else:

@@ -38,6 +38,19 @@ struct KinTables {
     void* k[3] = {nullptr, nullptr, nullptr};
 };
 
+// Dynamic potential mode (wfs_set_dynamic_walls): the walls with their current centres and
+// velocities, the absorbing ramp the rebuild adds, and the walls' slit axes on the device.
+struct DynWalls {
+    int nwall = 0;
+    wfs_wall walls[wfs::kMaxDynWalls];
+    double vel[wfs::kMaxDynWalls][3];
+    bool has_abs = false;
+    wfs_absorbing abs;
+    bool rebuilt = false;  // the first update rebuilds V whole, as the reference does every step
+    float* frames = nullptr;
+    wfs::WallDev* dwalls = nullptr;
+};
+
 }  // namespace
 
 namespace wfs {
@@ -63,6 +76,7 @@ struct wfs_handle {
     bool ephase_valid;
     void* tw[3];          // twiddle tables per axis
     KinTables kin_half, kin_full;
+    DynWalls dyn;
     Rep rep;
     double pend_dt, pend_mass;
     double* partials;     // observation scratch, per-CTA FP64 sums
@@ -350,6 +364,86 @@ bool fft_ready(wfs_handle* h) {
     return true;
 }
 
+// One update of the dynamic potential after a step (sources/sim_state.py:466-509): every
+// wall advects by v dt with its x centre clamped at 0, then V is rebuilt from the walls and
+// the absorbing ramp (sources/potential.py:508-522). The first update rebuilds V whole
+// (any pre-initialised potential is dropped, as in the reference); later ones rewrite only
+// the voxels a moving wall reached before or reaches after the move, together with their
+// phase-table entries, which gives the same V as a whole rebuild.
+template <typename R>
+int dyn_update(wfs_handle* h, double dt) {
+    DynWalls& d = h->dyn;
+    DynWallsDev dd;
+    std::memset(&dd, 0, sizeof(dd));
+    dd.nwall = d.nwall;
+    dd.frames = d.frames;
+    bool any = false;
+    for (int i = 0; i < d.nwall; ++i) {
+        wfs_wall& w = d.walls[i];
+        for (int k = 0; k < 3; ++k) dd.old_c[i][k] = float(w.center[k]);
+        for (int k = 0; k < 3; ++k) w.center[k] = w.center[k] + d.vel[i][k] * dt;
+        if (w.center[0] < 0.0) w.center[0] = 0.0;
+        if (!wall_frame(&w, dd.w[i])) return set_err(h, WFS_ERR_ARG, "invalid moving wall");
+        dd.moving[i] = (dd.w[i].cx != dd.old_c[i][0] || dd.w[i].cy != dd.old_c[i][1] || dd.w[i].cz != dd.old_c[i][2]);
+        any = any || dd.moving[i];
+    }
+    const float dx[3] = {float(h->dx[0]), float(h->dx[1]), float(h->dx[2])};
+    if (!d.rebuilt) {
+        PassScope ps(h, WFS_PASS_OTHER);
+        CK(cudaMemsetAsync(h->V, 0, h->count * sizeof(float2), h->stream));
+        for (int i = 0; i < d.nwall; ++i) CK(launch_wall(h->V, h->n, dx, dd.w[i], h->stream));
+        if (d.has_abs) {
+            AbsorbDev ad;
+            for (int k = 0; k < 3; ++k) {
+                ad.bottom[k] = float(d.abs.bottom[k]);
+                ad.top[k] = float(d.abs.top[k]);
+                ad.pp[k] = float(d.abs.potential_pos[k]);
+                ad.pn[k] = float(d.abs.potential_neg[k]);
+                ad.ep[k] = float(d.abs.exponent_pos[k]);
+                ad.en[k] = float(d.abs.exponent_neg[k]);
+            }
+            ad.offset = float(d.abs.offset);
+            CK(launch_absorbing(h->V, h->n, dx, ad, h->stream));
+        }
+        h->ephase_valid = false;
+        d.rebuilt = true;
+        return WFS_OK;
+    }
+    if (!any) return WFS_OK;
+    // the box the moving walls' bands lie in: along the normal of an axis-aligned wall the
+    // voxels within its reach of the old or new centre (one voxel of margin each side),
+    // the whole axis otherwise
+    for (int k = 0; k < 3; ++k) {
+        dd.lo[k] = h->n[k];
+        dd.hi[k] = -1;
+    }
+    for (int i = 0; i < d.nwall; ++i) {
+        if (!dd.moving[i]) continue;
+        const WallDev& w = dd.w[i];
+        const float nv[3] = {w.nx, w.ny, w.nz};
+        const float cn[3] = {w.cx, w.cy, w.cz};
+        const double reach = std::max(0.5 * w.plateau, 0.5 * w.plateau + double(w.slope));
+        for (int k = 0; k < 3; ++k) {
+            const bool aligned = nv[(k + 1) % 3] == 0.0f && nv[(k + 2) % 3] == 0.0f;
+            int lo = 0, hi = h->n[k] - 1;
+            if (aligned) {
+                const double c0 = std::min(double(cn[k]), double(dd.old_c[i][k]));
+                const double c1 = std::max(double(cn[k]), double(dd.old_c[i][k]));
+                const double v0 = std::floor((c0 - reach) / h->dx[k] + 0.5 * h->n[k]) - 1.0;
+                const double v1 = std::ceil((c1 + reach) / h->dx[k] + 0.5 * h->n[k]) + 1.0;
+                lo = int(std::max(0.0, std::min(v0, double(h->n[k] - 1))));
+                hi = int(std::max(0.0, std::min(v1, double(h->n[k] - 1))));
+            }
+            dd.lo[k] = std::min(dd.lo[k], lo);
+            dd.hi[k] = std::max(dd.hi[k], hi);
+        }
+    }
+    Cx<R>* e = (h->ephase_valid && h->ephase) ? reinterpret_cast<Cx<R>*>(h->ephase) : nullptr;
+    PassScope ps(h, WFS_PASS_OTHER);
+    CK(launch_wall_band<R>(h->V, e, h->ephase_dt, h->n, dx, dd, h->stream));
+    return WFS_OK;
+}
+
 template <typename R>
 int split_steps(wfs_handle* h, int nsteps, double dt, double mass) {
     if (nsteps <= 0) return WFS_OK;
@@ -374,6 +468,10 @@ int split_steps(wfs_handle* h, int nsteps, double dt, double mass) {
             if ((rc = pass_y<R>(h, -1))) return rc;
         }
         merged = true;
+        if (h->dyn.nwall) {  // the potential of the next step (update_potential after evolve_state)
+            if ((rc = dyn_update<R>(h, dt))) return rc;
+            if ((rc = ensure_ephase<R>(h, dt))) return rc;
+        }
     }
     h->rep = REP_PENDING;
     h->pend_dt = dt;
@@ -553,6 +651,7 @@ int taylor_steps(wfs_handle* h, int nsteps, double dt, double mass, int order, i
         // new psi = B; old psi and A become scratch
         h->scratch[1] = h->psi;
         h->psi = B;
+        if (h->dyn.nwall && (rc = dyn_update<R>(h, dt))) return rc;
     }
     return WFS_OK;
 }
@@ -662,7 +761,7 @@ int wfs_destroy(wfs_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     void* bufs[] = {h->psi, h->scratch[0], h->scratch[1], h->V, h->ephase, h->partials, h->series, h->dres, h->dflag,
                     h->tw[0], h->tw[1], h->tw[2], h->kin_half.k[0], h->kin_half.k[1], h->kin_half.k[2],
-                    h->kin_full.k[0], h->kin_full.k[1], h->kin_full.k[2]};
+                    h->kin_full.k[0], h->kin_full.k[1], h->kin_full.k[2], h->dyn.frames, h->dyn.dwalls};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h->hres) cudaFreeHost(h->hres);
@@ -724,6 +823,42 @@ int wfs_potential_add_absorbing(wfs_handle* h, const wfs_absorbing* a) {
     float dx[3] = {float(h->dx[0]), float(h->dx[1]), float(h->dx[2])};
     CK(launch_absorbing(h->V, h->n, dx, ad, h->stream));
     h->ephase_valid = false;
+    return WFS_OK;
+}
+
+int wfs_set_dynamic_walls(wfs_handle* h, const wfs_wall* walls, const double* velocity, int32_t nwall,
+                          const wfs_absorbing* absorbing) {
+    if (!h) return dispatch_err(h);
+    if (nwall < 0 || nwall > kMaxDynWalls)
+        return set_err(h, WFS_ERR_ARG, "nwall must be in [0, " + std::to_string(kMaxDynWalls) + "]");
+    if (nwall > 0 && (!walls || !velocity)) return set_err(h, WFS_ERR_ARG, "null walls or velocities");
+    DynWalls& d = h->dyn;
+    WallDev wd[kMaxDynWalls];
+    for (int i = 0; i < nwall; ++i)
+        if (!wall_frame(&walls[i], wd[i])) return set_err(h, WFS_ERR_ARG, "invalid wall " + std::to_string(i));
+    d.nwall = 0;
+    d.rebuilt = false;
+    if (nwall == 0) return WFS_OK;
+    if (!d.frames) CK(cudaMalloc(&d.frames, 3 * kMaxDynWalls * sizeof(float)));
+    if (!d.dwalls) CK(cudaMalloc(&d.dwalls, kMaxDynWalls * sizeof(WallDev)));
+    CK(cudaMemcpyAsync(d.dwalls, wd, nwall * sizeof(WallDev), cudaMemcpyHostToDevice, h->stream));
+    CK(launch_wall_frames(d.frames, d.dwalls, nwall, h->stream));
+    CK(cudaStreamSynchronize(h->stream));  // wd lives on this stack frame
+    for (int i = 0; i < nwall; ++i) {
+        d.walls[i] = walls[i];
+        for (int k = 0; k < 3; ++k) d.vel[i][k] = velocity[3 * i + k];
+    }
+    d.has_abs = absorbing != nullptr;
+    if (absorbing) d.abs = *absorbing;
+    d.nwall = nwall;
+    return WFS_OK;
+}
+
+int wfs_get_dynamic_walls(wfs_handle* h, double* centers, int32_t nwall) {
+    if (!h) return dispatch_err(h);
+    if (!centers || nwall != h->dyn.nwall) return set_err(h, WFS_ERR_ARG, "centers must hold 3 values per dynamic wall");
+    for (int i = 0; i < nwall; ++i)
+        for (int k = 0; k < 3; ++k) centers[3 * i + k] = h->dyn.walls[i].center[k];
     return WFS_OK;
 }
 

@@ -54,6 +54,46 @@ __device__ void wall_right(const WallDev& w, float r[3]) {
     for (int i = 0; i < 3; ++i) r[i] = fma_(Q[i][2], rt[2], fma_(Q[i][0], rt[0], fm(Q[i][1], rt[1])));
 }
 
+// Voxel position dx * (v - N/2) of potential_wall.cu:34 (transform_corner_origin_to_center_origin_system).
+__device__ __forceinline__ float wall_coord(int v, int n, float d) { return fm(d, fs(float(v), fm(0.5f, float(n)))); }
+
+// Distance of the voxel at r from the wall's mid-plane, |n.(r - c)|.
+__device__ __forceinline__ float wall_distance(const WallDev& w, float cx, float cy, float cz, float rx, float ry,
+                                               float rz) {
+    return fabsf(dot3c(w.nx, w.ny, w.nz, fs(rx, cx), fs(ry, cy), fs(rz, cz)));
+}
+
+// Adds the wall's value at r to acc (potential_wall.cu:46-82): nothing inside a slit or
+// beyond the slope, U on the plateau, U (1 - (d - p/2)/s)^e on the slope.
+__device__ __forceinline__ float wall_add(const WallDev& w, const float right[3], float acc, float rx, float ry,
+                                          float rz) {
+    const float ax = fs(rx, w.cx), ay = fs(ry, w.cy), az = fs(rz, w.cz);
+    const float d = fabsf(dot3c(w.nx, w.ny, w.nz, ax, ay, az));
+    const float dR = fabsf(dot3c(right[0], right[1], right[2], ax, ay, az));
+    const float sw = w.slit_width, sp = w.slit_spacing;
+    bool skip = false;
+    switch (w.slit_count) {
+        case 1: skip = dR < fm(sw, 0.5f); break;
+        case 2: skip = dR > fm(fs(sp, sw), 0.5f) && dR < fm(fa(sp, sw), 0.5f); break;
+        case 3:
+            skip = (dR < fm(sw, 0.5f)) || (dR > fs(sp, fm(sw, 0.5f)) && dR < fa(sp, fm(sw, 0.5f)));
+            break;
+        case 4:
+            skip = (dR > fm(fs(sp, sw), 0.5f) && dR < fm(fa(sp, sw), 0.5f)) ||
+                   (dR > fma_(sp, 1.5f, -fm(sw, 0.5f)) && dR < fma_(sp, 1.5f, fm(sw, 0.5f)));
+            break;
+        default: break;
+    }
+    if (skip) return acc;
+    const float p2 = fm(w.plateau, 0.5f);
+    if (d <= p2) return fa(acc, w.U);
+    if (d <= fa(p2, w.slope)) {
+        const float tt = fs(1.0f, __fdiv_rn(fs(d, p2), w.slope));
+        return fa(acc, fm(w.U, powf(tt, w.slope_exp)));
+    }
+    return acc;
+}
+
 __global__ void wall_kernel(float2* __restrict__ V, int nx, int ny, int nz, float dxx, float dxy, float dxz, WallDev w) {
     const int64_t total = int64_t(nx) * ny * nz;
     float right[3];
@@ -62,34 +102,10 @@ __global__ void wall_kernel(float2* __restrict__ V, int nx, int ny, int nz, floa
         const int z = int(idx % nz);
         const int y = int((idx / nz) % ny);
         const int x = int(idx / (int64_t(ny) * nz));
-        const float rx = fm(dxx, fs(float(x), fm(0.5f, float(nx))));
-        const float ry = fm(dxy, fs(float(y), fm(0.5f, float(ny))));
-        const float rz = fm(dxz, fs(float(z), fm(0.5f, float(nz))));
-        const float ax = fs(rx, w.cx), ay = fs(ry, w.cy), az = fs(rz, w.cz);
-        const float d = fabsf(dot3c(w.nx, w.ny, w.nz, ax, ay, az));
-        const float dR = fabsf(dot3c(right[0], right[1], right[2], ax, ay, az));
-        const float sw = w.slit_width, sp = w.slit_spacing;
-        bool skip = false;
-        switch (w.slit_count) {
-            case 1: skip = dR < fm(sw, 0.5f); break;
-            case 2: skip = dR > fm(fs(sp, sw), 0.5f) && dR < fm(fa(sp, sw), 0.5f); break;
-            case 3:
-                skip = (dR < fm(sw, 0.5f)) || (dR > fs(sp, fm(sw, 0.5f)) && dR < fa(sp, fm(sw, 0.5f)));
-                break;
-            case 4:
-                skip = (dR > fm(fs(sp, sw), 0.5f) && dR < fm(fa(sp, sw), 0.5f)) ||
-                       (dR > fma_(sp, 1.5f, -fm(sw, 0.5f)) && dR < fma_(sp, 1.5f, fm(sw, 0.5f)));
-                break;
-            default: break;
-        }
-        if (skip) continue;
-        const float p2 = fm(w.plateau, 0.5f);
-        if (d <= p2) {
-            V[idx].x = fa(V[idx].x, w.U);
-        } else if (d <= fa(p2, w.slope)) {
-            const float tt = fs(1.0f, __fdiv_rn(fs(d, p2), w.slope));
-            V[idx].x = fa(V[idx].x, fm(w.U, powf(tt, w.slope_exp)));
-        }
+        const float rx = wall_coord(x, nx, dxx), ry = wall_coord(y, ny, dxy), rz = wall_coord(z, nz, dxz);
+        const float v0 = V[idx].x;
+        const float v1 = wall_add(w, right, v0, rx, ry, rz);
+        if (v1 != v0 || __float_as_uint(v1) != __float_as_uint(v0)) V[idx].x = v1;
     }
 }
 
@@ -100,6 +116,73 @@ cudaError_t launch_wall(float2* V, const int n[3], const float dx[3], const Wall
     wall_kernel<<<grid, 256, 0, s>>>(V, n[0], n[1], n[2], dx[0], dx[1], dx[2], w);
     return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Dynamic potential mode (sources/sim_state.py:466-509, sources/potential.py:508-522):
+// after each step the moving walls advect and V is rebuilt from the walls and the
+// absorbing ramp. Only voxels within a moving wall's reach (plateau/2 + slope) before or
+// after the move can change; this kernel recomputes V.x there as the rebuild does (zero,
+// then every wall in order) and refreshes the phase table entry with vphase's formula.
+// ---------------------------------------------------------------------------
+__global__ void wall_frames_kernel(float* __restrict__ frames, const WallDev* __restrict__ walls, int nwall) {
+    const int i = threadIdx.x;
+    if (i < nwall) wall_right(walls[i], frames + 3 * i);
+}
+
+cudaError_t launch_wall_frames(float* frames, const WallDev* walls, int nwall, cudaStream_t s) {
+    wall_frames_kernel<<<1, 32, 0, s>>>(frames, walls, nwall);
+    return cudaGetLastError();
+}
+
+template <typename R>
+__device__ __forceinline__ Cx<R> vphase_one(float2 v, R dt);
+
+template <typename R>
+__global__ void __launch_bounds__(256) wall_band_kernel(float2* __restrict__ V, Cx<R>* __restrict__ e, R dt, int nx,
+                                                        int ny, int nz, float dxx, float dxy, float dxz,
+                                                        const DynWallsDev d) {
+    // one thread per voxel of the box d.lo..d.hi: z from the thread, y and x from the grid
+    const int z = d.lo[2] + int(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = d.lo[1] + int(blockIdx.y);
+    const int x = d.lo[0] + int(blockIdx.z);
+    if (z > d.hi[2]) return;
+    const float rx = wall_coord(x, nx, dxx), ry = wall_coord(y, ny, dxy), rz = wall_coord(z, nz, dxz);
+    bool touched = false;
+    for (int i = 0; i < d.nwall && !touched; ++i) {
+        if (!d.moving[i]) continue;
+        const WallDev& w = d.w[i];
+        const float p2 = fm(w.plateau, 0.5f);
+        const float reach = fmaxf(p2, fa(p2, w.slope));
+        touched = wall_distance(w, w.cx, w.cy, w.cz, rx, ry, rz) <= reach ||
+                  wall_distance(w, d.old_c[i][0], d.old_c[i][1], d.old_c[i][2], rx, ry, rz) <= reach;
+    }
+    if (!touched) return;
+    float vr = 0.0f;
+    for (int i = 0; i < d.nwall; ++i) {
+        const float right[3] = {d.frames[3 * i], d.frames[3 * i + 1], d.frames[3 * i + 2]};
+        vr = wall_add(d.w[i], right, vr, rx, ry, rz);
+    }
+    const int64_t idx = (int64_t(x) * ny + y) * nz + z;
+    float2 v = V[idx];
+    v.x = vr;
+    V[idx] = v;
+    if (e) e[idx] = vphase_one<R>(v, dt);
+}
+
+template <typename R>
+cudaError_t launch_wall_band(float2* V, Cx<R>* e, double dt, const int n[3], const float dx[3], const DynWallsDev& d,
+                             cudaStream_t s) {
+    const int nzb = d.hi[2] - d.lo[2] + 1, nyb = d.hi[1] - d.lo[1] + 1, nxb = d.hi[0] - d.lo[0] + 1;
+    if (nzb < 1 || nyb < 1 || nxb < 1) return cudaSuccess;
+    const int block = nzb < 256 ? ((nzb + 31) / 32) * 32 : 256;
+    const dim3 grid(unsigned((nzb + block - 1) / block), unsigned(nyb), unsigned(nxb));
+    wall_band_kernel<R><<<grid, block, 0, s>>>(V, e, R(dt), n[0], n[1], n[2], dx[0], dx[1], dx[2], d);
+    return cudaGetLastError();
+}
+template cudaError_t launch_wall_band<float>(float2*, Cx<float>*, double, const int*, const float*, const DynWallsDev&,
+                                             cudaStream_t);
+template cudaError_t launch_wall_band<double>(float2*, Cx<double>*, double, const int*, const float*,
+                                              const DynWallsDev&, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Absorbing boundary — absorbing_potential.cu:37-306
@@ -341,17 +424,21 @@ template cudaError_t launch_gaussian<double>(Cx<double>*, const int*, const doub
 // Potential phase table e = cexp_i(-dt V) = e^{-i dt ReV} e^{dt ImV}
 // (potential_operator.cu:11-15, common.cu:98-111), in the wave function's precision.
 // ---------------------------------------------------------------------------
+// exp(-i dt V) = (cos(-dt Vr), sin(-dt Vr)) exp(dt Vi) (potential_operator.cu:11-15, common.cu:98-111)
+template <typename R>
+__device__ __forceinline__ Cx<R> vphase_one(float2 v, R dt) {
+    const R re = -dt * R(v.x);
+    const R im = -dt * R(v.y);
+    R s, c;
+    sincos_r(re, &s, &c);
+    const R m = exp_r(-im);
+    return mk<R>(c * m, s * m);
+}
+
 template <typename R>
 __global__ void vphase_kernel(Cx<R>* __restrict__ e, const float2* __restrict__ V, R dt, int64_t count) {
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
-        const float2 v = V[i];
-        const R re = -dt * R(v.x);
-        const R im = -dt * R(v.y);
-        R s, c;
-        sincos_r(re, &s, &c);
-        const R m = exp_r(-im);
-        e[i] = mk<R>(c * m, s * m);
-    }
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
+        e[i] = vphase_one<R>(V[i], dt);
 }
 template <typename R>
 cudaError_t launch_vphase(Cx<R>* e, const float2* V, double dt, int64_t count, cudaStream_t s) {

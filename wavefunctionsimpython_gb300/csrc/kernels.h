@@ -121,6 +121,26 @@ struct AbsorbDev {
 };
 
 cudaError_t launch_wall(float2* V, const int n[3], const float dx[3], const WallDev& w, cudaStream_t s);
+
+// Moving walls of the dynamic potential mode: every wall at its current centre, plus the
+// previous centres of the walls that move. frames[3 * i] is wall i's rotated slit axis
+// (wall_right), formed once on the device by launch_wall_frames.
+constexpr int kMaxDynWalls = 8;
+struct DynWallsDev {
+    int nwall;
+    WallDev w[kMaxDynWalls];          // centre = the centre after this step's advection
+    float old_c[kMaxDynWalls][3];     // centre before it
+    int moving[kMaxDynWalls];         // 1 when the wall moved this step
+    int lo[3], hi[3];                 // voxel box (inclusive) that holds every moving wall's band
+    const float* frames;
+};
+cudaError_t launch_wall_frames(float* frames, const WallDev* walls, int nwall, cudaStream_t s);
+// Rewrites V.x (the sum of all walls, in order, from zero) and the phase table e at the
+// voxels that a moving wall covered before or covers after this step; other voxels keep
+// their values, which the walls' new positions do not change. e may be null (no table).
+template <typename R>
+cudaError_t launch_wall_band(float2* V, Cx<R>* e, double dt, const int n[3], const float dx[3], const DynWallsDev& d,
+                             cudaStream_t s);
 cudaError_t launch_absorbing(float2* V, const int n[3], const float dx[3], const AbsorbDev& a, cudaStream_t s);
 cudaError_t launch_add_raw(float2* V, const void* src, int raw_type, int64_t count, cudaStream_t s);
 template <typename R>

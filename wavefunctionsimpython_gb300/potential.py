@@ -62,14 +62,17 @@ class AbsorbingBoundaryCondition:
             try_read_param(config, p + "slope_exponent_in_negative_xyz_direction_3", [2.0] * 3))
         self.enable = try_read_param(config, p + "enable", True)
 
+    def engine_args(self):
+        """The seven Engine.add_absorbing arguments."""
+        return (self.boundary_bottom_corner_bohr_radii_3, self.boundary_top_corner_bohr_radii_3,
+                self.start_offset, self.outer_potential_in_positive_xyz_direction_hartree_3,
+                self.outer_potential_in_negative_xyz_direction_hartree_3,
+                self.slope_exponent_in_positive_xyz_direction_3, self.slope_exponent_in_negative_xyz_direction_3)
+
     def add_potential(self, engine):
         if not self.enable:
             return
-        engine.add_absorbing(self.boundary_bottom_corner_bohr_radii_3, self.boundary_top_corner_bohr_radii_3,
-                             self.start_offset, self.outer_potential_in_positive_xyz_direction_hartree_3,
-                             self.outer_potential_in_negative_xyz_direction_hartree_3,
-                             self.slope_exponent_in_positive_xyz_direction_3,
-                             self.slope_exponent_in_negative_xyz_direction_3)
+        engine.add_absorbing(*self.engine_args())
 
 
 class PotentialWall:
@@ -104,13 +107,16 @@ class PotentialWall:
     def is_moving(self):
         return bool(np.any(self.velocity_bohr_radius_hartree_per_h_bar_3 != 0.0))
 
+    def engine_args(self):
+        """The ten Engine.add_wall arguments."""
+        return (self.potential_hartree, self.center_bohr_radii_3, self.normal_vector_3,
+                self.plateau_thickness_bohr_radii, self.slope_thickness_bohr_radii, self.slope_exponent,
+                self.slit_count, self.slit_spacing_bohr_radii, self.slit_width_bohr_radii, self.slit_rotation_radian)
+
     def add_potential(self, engine):
         if not self.enable:
             return
-        engine.add_wall(self.potential_hartree, self.center_bohr_radii_3, self.normal_vector_3,
-                        self.plateau_thickness_bohr_radii, self.slope_thickness_bohr_radii, self.slope_exponent,
-                        self.slit_count, self.slit_spacing_bohr_radii, self.slit_width_bohr_radii,
-                        self.slit_rotation_radian)
+        engine.add_wall(*self.engine_args())
 
 
 def generate_potential_from_walls_and_drain(engine, absorbing: AbsorbingBoundaryCondition, walls):

@@ -109,6 +109,7 @@ class SimState:
         # per-instance wall list (the reference shares a class-level list between instances)
         self.__potential_walls = [potential.PotentialWall(w) for w in try_read_param(config, "potential.walls", [])]
         self.__use_cache = True
+        self.__engine_dynamic_walls = False
         self.engine: Engine | None = None
 
     # ------------------------------------------------------------------ init
@@ -154,6 +155,7 @@ class SimState:
                 os.path.join(self.__output_dir, "potential_raw", "potential.bin"))
         except OSError as e:
             print(f"Failed writing potential.bin: {e}")
+        self._register_dynamic_walls()
 
     @staticmethod
     def _try_save(path, getter):
@@ -270,25 +272,41 @@ class SimState:
         return float(np.prod(self.__delta_x_bohr_radii_3))
 
     # ---------------------------------------------------------- evolution
+    def _enabled_walls(self):
+        return [w for w in self.__potential_walls if w.enable]
+
+    def _register_dynamic_walls(self):
+        """Dynamic potential mode (sources/sim_state.py:466-509): the engine is given the
+        enabled walls with their velocities and the absorbing ramp, and after every step it
+        advects the walls (x clamped at 0) and rebuilds V on the device, so stepping never
+        returns to the host for it. Without a moving wall the rebuild would reproduce V
+        unchanged (no pre-initialised potential exists in this mode), so nothing is set."""
+        self.__engine_dynamic_walls = False
+        if self.engine is None or not self.has_moving_potential():
+            return
+        walls = self._enabled_walls()
+        ab = self.__absorbing_boundary_condition
+        self.engine.set_dynamic_walls([w.engine_args() for w in walls],
+                                      [w.velocity_bohr_radius_hartree_per_h_bar_3 for w in walls],
+                                      ab.engine_args() if ab.enable else None)
+        self.__engine_dynamic_walls = True
+
+    def sync_dynamic_walls(self):
+        """Copies the engine's current wall centres back into the wall objects."""
+        if self.__engine_dynamic_walls:
+            for w, c in zip(self._enabled_walls(), self.engine.get_dynamic_walls()):
+                w.center_bohr_radii_3 = np.array(c, dtype=np.float64)
+
     def update_potential(self):
-        """sources/sim_state.py:466-509: in dynamic mode walls advect by v*dt (x clamped
-        at 0) and V is rebuilt on the GPU. V is only rebuilt when a wall moved, since
-        rebuilding an unchanged V gives the same array."""
+        """sources/sim_state.py:466-509. In dynamic mode the engine has already advected
+        the moving walls and rebuilt V after each step of evolve_state; the walls' new
+        centres are read back here."""
         if not self.__is_dynamic_potential_mode:
             return
-        moved = False
-        for w in self.__potential_walls:
-            if w.is_moving():
-                w.center_bohr_radii_3 = w.center_bohr_radii_3 + w.velocity_bohr_radius_hartree_per_h_bar_3 * self.__delta_time_h_bar_per_hartree
-                if w.center_bohr_radii_3[0] < 0.0:
-                    w.center_bohr_radii_3[0] = 0.0
-                moved = True
-        if moved:
-            potential.generate_potential_from_walls_and_drain(self.engine, self.__absorbing_boundary_condition,
-                                                              self.__potential_walls)
+        self.sync_dynamic_walls()
 
     def has_moving_potential(self) -> bool:
-        return self.__is_dynamic_potential_mode and any(w.is_moving() for w in self.__potential_walls)
+        return self.__is_dynamic_potential_mode and any(w.enable and w.is_moving() for w in self.__potential_walls)
 
     def evolve_state(self, nsteps: int = 1):
         """sources/sim_state.py:754-762 — one (or nsteps) step(s) of the configured method."""
@@ -306,6 +324,7 @@ class SimState:
         a run resumes exactly where it stopped. The reference has no working psi
         checkpoint (its snapshot writer is commented out, sources/snapshot_io.py:12-16)."""
         eng = self.engine
+        self.sync_dynamic_walls()
         walls = np.array([np.concatenate([w.center_bohr_radii_3, w.velocity_bohr_radius_hartree_per_h_bar_3,
                                           [float(w.potential_hartree)]]) for w in self.__potential_walls],
                          dtype=np.float64).reshape(-1, 7)
@@ -339,6 +358,7 @@ class SimState:
                 w.center_bohr_radii_3 = row[0:3].copy()
                 w.velocity_bohr_radius_hartree_per_h_bar_3 = row[3:6].copy()
                 w.potential_hartree = float(row[6])
+            self._register_dynamic_walls()
             if iter_data is not None:
                 iter_data.i = int(f["iteration"][0])
                 iter_data.total_simulated_time = float(f["times"][0])
