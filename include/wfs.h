@@ -159,6 +159,25 @@ int wfs_run_split(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t
                   const wfs_box* boxes, int32_t nbox, const wfs_box* loc,
                   double* prob_series, double* loc_series);
 
+/* Sampling plane of a probability current (PlaneProbabilityCurrent,
+ * sources/measurement.py:190-256): centre and normal in Bohr radii, extent
+ * size[2] and odd Simpson sample counts count[2]. */
+typedef struct {
+    double center[3];
+    double normal[3];
+    double size[2];
+    int32_t count[2];
+} wfs_plane;
+
+/* wfs_run_split plus plane probability currents: before every interval-th step
+ * the flux through each plane is recorded too, flux_series[rec*nplane + p], all
+ * on the device (MeasurementTools.measure_and_render with plane currents,
+ * sources/measurement.py:644-705). With planes, the observables are taken from
+ * real-space psi. */
+int wfs_run_split_planes(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t interval,
+                         const wfs_box* boxes, int32_t nbox, const wfs_box* loc, const wfs_plane* planes,
+                         int32_t nplane, double* prob_series, double* loc_series, double* flux_series);
+
 /* Probability flux through a sampled plane: PlaneProbabilityCurrent.calculate
  * (sources/measurement.py:258-289, probability_current_density.cu:11-218).
  * count[2] are the (odd) Simpson sample counts, size[2] the plane's extent in

@@ -227,3 +227,31 @@ def test_maximum_sizes_keep_norm_and_reverse(n):
     np.testing.assert_allclose(r2, r0, atol=1e-4)
     np.testing.assert_allclose(q2, q0, rtol=1e-4)
     e.close()
+
+
+def test_observables_at_256_accurate_to_1e9(slit):
+    """Compensated (float-float) thread and warp sums with FP64 CTA and grid sums: at 256^3
+    complex64 the volume probabilities and <r>, <r^2> from both observation paths (the
+    fused transform after split steps and the real-space kernel) agree with FP64 sums
+    of the same psi to 1e-9."""
+    e = engine_for(slit)
+    e.step_split(10, slit.dt, 1.0)
+    inner = 40.0 - 16 * slit.dx[0]
+    trans = orc.simpson_box_from_corners((1.0, -inner, -inner), (inner, inner, inner), slit.extent, slit.n)
+    obsb = orc.simpson_box_from_corners((-inner,) * 3, (inner,) * 3, slit.extent, slit.n)
+    left = orc.simpson_box_from_corners((-inner,) * 3, (0.0, inner, inner), slit.extent, slit.n)
+    boxes = [tuple(map(tuple, b)) for b in (trans, obsb, left)]
+    fused = e.observe(boxes, boxes[1])  # from the split step's frequency-space state
+    psi = e.get_psi()
+    real = e.observe(boxes, boxes[1])   # from real-space psi
+    ref_p = [orc.volume_probability(psi, slit.dx, *b) for b in boxes]
+    ref_r, ref_r2 = orc.expected_location(psi, slit.dx, *boxes[1])
+    scale_r = float(np.sqrt(np.max(ref_r2)))
+    for name, (probs, r, r2) in (("fused", fused), ("real", real)):
+        print(name, "probabilities", np.abs(np.asarray(probs) / np.asarray(ref_p) - 1.0),
+              "<r>", np.abs(r - ref_r) / scale_r, "<r^2>", np.abs(r2 / ref_r2 - 1.0))
+        np.testing.assert_allclose(probs[1:], ref_p[1:], rtol=1e-9)
+        assert abs(probs[0] - ref_p[0]) < 1e-9 * ref_p[1]  # P(x > 1) is still ~0 after 10 steps
+        np.testing.assert_allclose(r, ref_r, rtol=0, atol=1e-9 * scale_r)
+        np.testing.assert_allclose(r2, ref_r2, rtol=1e-9)
+    e.close()

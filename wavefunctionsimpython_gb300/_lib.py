@@ -33,7 +33,7 @@ EXPORTED = [
     "wfs_potential_clear", "wfs_potential_add_wall", "wfs_potential_add_absorbing", "wfs_potential_add_raw",
     "wfs_set_potential", "wfs_get_potential", "wfs_set_dynamic_walls", "wfs_get_dynamic_walls", "wfs_init_gaussian", "wfs_set_psi", "wfs_get_psi",
     "wfs_psi_device_ptr", "wfs_step_split", "wfs_step_taylor", "wfs_kinetic_operator", "wfs_potential_operator",
-    "wfs_observe", "wfs_run_split", "wfs_norm", "wfs_profile_enable", "wfs_profile_read", "wfs_launch_count",
+    "wfs_observe", "wfs_run_split", "wfs_run_split_planes", "wfs_norm", "wfs_profile_enable", "wfs_profile_read", "wfs_launch_count",
     "wfs_set_schedule", "wfs_split_step_gain",
     "wfs_batch_create", "wfs_batch_destroy", "wfs_batch_last_error", "wfs_batch_synchronize",
     "wfs_batch_init_gaussian", "wfs_batch_add_wall", "wfs_batch_add_absorbing", "wfs_batch_set_potential",
@@ -69,6 +69,11 @@ class WallDesc(C.Structure):
                 ("plateau_thickness", C.c_double), ("slope_thickness", C.c_double), ("slope_exponent", C.c_double),
                 ("slit_count", C.c_int32), ("slit_spacing", C.c_double), ("slit_width", C.c_double),
                 ("slit_rotation", C.c_double)]
+
+
+class PlaneDesc(C.Structure):
+    _fields_ = [("center", C.c_double * 3), ("normal", C.c_double * 3), ("size", C.c_double * 2),
+                ("count", C.c_int32 * 2)]
 
 
 class AbsorbingDesc(C.Structure):
@@ -147,6 +152,8 @@ def load(path: str | os.PathLike | None = None):
         "wfs_potential_operator": ([vp, dbl, vp, i32], C.c_int),
         "wfs_observe": ([vp, C.POINTER(Box), i32, C.POINTER(Box), dp, dp, dp], C.c_int),
         "wfs_run_split": ([vp, i32, dbl, dbl, i32, C.POINTER(Box), i32, C.POINTER(Box), dp, dp], C.c_int),
+        "wfs_run_split_planes": ([vp, i32, dbl, dbl, i32, C.POINTER(Box), i32, C.POINTER(Box), C.POINTER(PlaneDesc),
+                                  i32, dp, dp, dp], C.c_int),
         "wfs_norm": ([vp, dp], C.c_int),
         "wfs_profile_enable": ([vp, i32], C.c_int),
         "wfs_profile_read": ([vp, dp, C.POINTER(C.c_int64), i32], C.c_int),
@@ -408,6 +415,28 @@ class Engine:
                                         ps.ctypes.data_as(C.POINTER(C.c_double)),
                                         ls.ctypes.data_as(C.POINTER(C.c_double))))
         return ps[:nrec, :nb], ls[:nrec]
+
+    def run_split_planes(self, nsteps, dt, mass=1.0, interval=1, boxes=(), loc=None, planes=()):
+        """run_split that also records, before every interval-th step, the probability flux
+        through each plane (center, normal, size[2], count[2]). Returns (probabilities,
+        locations, fluxes[nrec, nplane])."""
+        arr, nb = self._boxes(boxes)
+        lb = make_box(*loc) if loc is not None else None
+        npl = len(planes)
+        parr = (PlaneDesc * max(npl, 1))()
+        for i, (c, nrm, size, count) in enumerate(planes):
+            parr[i] = PlaneDesc(_d3(c), _d3(nrm), (C.c_double * 2)(*[float(x) for x in size]),
+                                (C.c_int32 * 2)(*[int(x) for x in count]))
+        nrec = -(-int(nsteps) // int(interval)) if (nb or lb is not None or npl) else 0
+        ps = np.zeros((max(nrec, 1), max(nb, 1)), dtype=np.float64)
+        ls = np.zeros((max(nrec, 1), 6), dtype=np.float64)
+        fs = np.zeros((max(nrec, 1), max(npl, 1)), dtype=np.float64)
+        self._ck(self.lib.wfs_run_split_planes(self.h, int(nsteps), float(dt), float(mass), int(interval), arr, nb,
+                                               C.byref(lb) if lb is not None else None, parr, npl,
+                                               ps.ctypes.data_as(C.POINTER(C.c_double)),
+                                               ls.ctypes.data_as(C.POINTER(C.c_double)),
+                                               fs.ctypes.data_as(C.POINTER(C.c_double))))
+        return ps[:nrec, :nb], ls[:nrec], fs[:nrec, :npl]
 
     def profile_enable(self, on=True, stride=1):
         """Bracket the launches of every ``stride``-th step with CUDA events (0/False: off)."""

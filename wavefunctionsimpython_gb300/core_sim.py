@@ -2,8 +2,9 @@
 
 ``time_step`` keeps the reference order (measure, evolve, update potential).
 ``run_iteration`` runs the whole loop on the device when every enabled
-measurement is a fused observable (volume probabilities and the expected
-location) and no wave function is saved: the engine then records the
+measurement is a fused observable (volume probabilities, the expected
+location and plane probability currents) and no wave function is saved: the
+engine then records the
 observables before each step, exactly as the per-step loop would, and in
 dynamic potential mode advects the walls and rebuilds V after each step,
 without a host round trip per step. Otherwise it steps from Python.
@@ -54,6 +55,7 @@ def run_iteration(sim_state: SimState, measurement_tools: MeasurementTools, iter
         total = int(iter_data.total_iteration_count)
         if _can_fuse(sim_state, measurement_tools):
             boxes, loc = measurement_tools.observation_request()
+            planes = measurement_tools.plane_request()
             dt = sim_state.get_delta_time_h_bar_per_hartree()
             m = sim_state.get_particle_mass()
             i = start
@@ -61,13 +63,20 @@ def run_iteration(sim_state: SimState, measurement_tools: MeasurementTools, iter
                 n = min(FUSED_CHUNK - FUSED_CHUNK % observation_interval if FUSED_CHUNK >= observation_interval
                         else observation_interval, total - i)
                 t0 = time.time()
-                probs, locs = sim_state.engine.run_split(n, dt, m, observation_interval, boxes, loc)
+                if planes:
+                    probs, locs, fluxes = sim_state.engine.run_split_planes(n, dt, m, observation_interval, boxes,
+                                                                            loc, planes)
+                else:
+                    probs, locs = sim_state.engine.run_split(n, dt, m, observation_interval, boxes, loc)
+                    fluxes = None
                 sim_state.engine.synchronize()
                 iter_data.elapsed_system_time_s += time.time() - t0
-                for k in range(probs.shape[0] if (boxes or loc is not None) else 0):
+                for k in range(probs.shape[0] if (boxes or loc is not None or planes) else 0):
                     er = locs[k, :3] if loc is not None else None
                     er2 = locs[k, 3:] if loc is not None else None
                     measurement_tools.record(probs[k] if boxes else [], er, er2)
+                    if fluxes is not None:
+                        measurement_tools.record_fluxes(fluxes[k])
                 sim_state.sync_dynamic_walls()
                 i += n
                 iter_data.i = i

@@ -7,9 +7,9 @@
 // voxel trunc(r/dx + N/2) (clamped to the grid; out-of-range stencil
 // neighbours are replaced by the centre, as in the reference). The density is
 //   j.n = (-hbar/2m) Re(i (psi* dpsi - psi dpsi*)) = Im(psi* dpsi) / m,
-// integrated with 2D Simpson weights; per-thread sums in the working
-// precision, block and grid sums in FP64 (deterministic order).
-#include "kernels.h"
+// integrated with 2D Simpson weights; per-thread and warp sums compensated
+// (CSum, fft_kernels.cuh), block and grid sums in FP64 (deterministic order).
+#include "fft_kernels.cuh"
 
 namespace wfs {
 
@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(256) plane_current_kernel(const Cx<R>* __restr
     __shared__ double red[32];
     const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
     const int64_t total = int64_t(a.sx) * a.sy;
-    R acc = R(0);  // thread and warp sums in the working precision, block sums in FP64
+    CSum<R> acc;
     for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < total; p += int64_t(gridDim.x) * blockDim.x) {
         const int px = int(p / a.sy), py = int(p % a.sy);
         const float ax = float(px - a.sx / 2), ay = float(py - a.sy / 2);
@@ -60,11 +60,12 @@ __global__ void __launch_bounds__(256) plane_current_kernel(const Cx<R>* __restr
         if (density) density[p] = dens;
         R wx = (px == 0 || px == a.sx - 1) ? R(1) : ((px & 1) ? R(4) : R(2));
         R wy = (py == 0 || py == a.sy - 1) ? R(1) : ((py & 1) ? R(4) : R(2));
-        acc += dens * wx * wy;
+        acc.add(dens * (wx * wy));
     }
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) acc.merge(acc.shfl_xor(m));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) red[warp] = double(acc);
+    if (lane == 0) red[warp] = acc.value();
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0.0;

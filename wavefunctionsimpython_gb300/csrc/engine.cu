@@ -548,10 +548,10 @@ void finish_obs(const wfs_handle* h, const ObsArgs& o, const double* raw, double
     for (int b = 0; b < o.nbox; ++b)
         if (prob) prob[b] = raw[b] * dv;
     if (o.has_loc) {
-        const double* l = raw + o.nbox;
+        const double* l = raw + o.nbox;  // sums of w (v - N/2) and w (v - N/2)^2 per axis
         for (int a = 0; a < 3; ++a) {
-            if (r) r[a] = l[1 + a] * dv;
-            if (r2) r2[a] = l[4 + a] * dv;
+            if (r) r[a] = l[1 + a] * h->dx[a] * dv;
+            if (r2) r2[a] = l[4 + a] * (h->dx[a] * h->dx[a]) * dv;
         }
     }
 }
@@ -572,15 +572,63 @@ int do_observe(wfs_handle* h, const wfs_box* boxes, int nbox, const wfs_box* loc
     return WFS_OK;
 }
 
+// Sampling plane of PlaneProbabilityCurrent (sources/measurement.py:207-289): frame, sample
+// grid and the sample spacings dW, dH the flux is scaled by.
+int fill_plane(wfs_handle* h, const double* center, const double* normal, const double* size, const int32_t* count,
+               double mass, PlaneCurrentArgs& a, double* dW, double* dH) {
+    if (!center || !normal || !size || !count || !(mass > 0)) return set_err(h, WFS_ERR_ARG, "invalid plane argument");
+    if (count[0] < 3 || count[1] < 3 || (count[0] % 2) == 0 || (count[1] % 2) == 0)
+        return set_err(h, WFS_ERR_ARG, "sample counts must be odd and >= 3 (Simpson)");
+    std::memset(&a, 0, sizeof(a));
+    if (!plane_frame(normal, a.normal, a.right, a.up)) return set_err(h, WFS_ERR_ARG, "degenerate plane normal");
+    for (int k = 0; k < 3; ++k) {
+        a.n[k] = h->n[k];
+        a.dx[k] = h->dx[k];
+        a.center[k] = float(center[k]);
+    }
+    a.sx = count[0];
+    a.sy = count[1];
+    a.mass = mass;
+    *dW = is_dbl(h) ? size[0] / double(a.sx - 1) : double(float(size[0]) / float(a.sx - 1));
+    *dH = is_dbl(h) ? size[1] / double(a.sy - 1) : double(float(size[1]) / float(a.sy - 1));
+    a.dWf = float(*dW);
+    a.dHf = float(*dH);
+    return WFS_OK;
+}
+
+// Arguments of every plane and the factor dW dH / 9 that turns its raw Simpson sum into a flux.
+int fill_planes(wfs_handle* h, const wfs_plane* planes, int nplane, double mass, std::vector<PlaneCurrentArgs>& pa,
+                std::vector<double>& pscale) {
+    pa.resize(size_t(nplane));
+    pscale.resize(size_t(nplane));
+    for (int i = 0; i < nplane; ++i) {
+        const wfs_plane& pl = planes[i];
+        double dW = 0, dH = 0;
+        const int rc = fill_plane(h, pl.center, pl.normal, pl.size, pl.count, mass, pa[size_t(i)], &dW, &dH);
+        if (rc) return rc;
+        pscale[size_t(i)] = dW * dH / 9.0;
+    }
+    return WFS_OK;
+}
+
+constexpr int kPlaneCurrentBlocks = 1024;  // CTAs (and FP64 partial sums) of a plane-current launch
+
 template <typename R>
 int do_run_split(wfs_handle* h, int nsteps, double dt, double mass, int interval, const wfs_box* boxes, int nbox,
-                 const wfs_box* loc, double* prob_series, double* loc_series) {
+                 const wfs_box* loc, double* prob_series, double* loc_series, const wfs_plane* planes = nullptr,
+                 int nplane = 0, double* flux_series = nullptr) {
     if (interval < 1) return set_err(h, WFS_ERR_ARG, "interval must be >= 1");
     ObsArgs o;
     int rc = fill_obs(h, boxes, nbox, loc, o);
     if (rc) return rc;
-    const int nrec = o.nq ? (nsteps + interval - 1) / interval : 0;
-    const size_t need = size_t(nrec) * o.nq;
+    if (nplane < 0 || (nplane > 0 && !planes)) return set_err(h, WFS_ERR_ARG, "invalid planes");
+    std::vector<PlaneCurrentArgs> pa;
+    std::vector<double> pscale;
+    if ((rc = fill_planes(h, planes, nplane, mass, pa, pscale))) return rc;
+    if (nplane && (rc = ensure_partials(h, kPlaneCurrentBlocks))) return rc;
+    const int stride = o.nq + nplane;  // doubles per record
+    const int nrec = stride ? (nsteps + interval - 1) / interval : 0;
+    const size_t need = size_t(nrec) * stride;
     if (need > h->series_cap) {  // kept across calls so repeated runs allocate nothing
         if (h->series) cudaFree(h->series);
         h->series = nullptr;
@@ -591,11 +639,24 @@ int do_run_split(wfs_handle* h, int nsteps, double dt, double mass, int interval
     double* dser = h->series;
     int rec = 0;
     for (int i = 0; i < nsteps && rc == WFS_OK; i += interval) {
-        if (o.nq) rc = observe_launch<R>(h, o, dser + size_t(rec++) * o.nq);
+        double* slot = dser + size_t(rec++) * stride;
+        // plane currents read real-space psi: observe from it too (no fused transform)
+        if (nplane) rc = to_real<R>(h);
+        if (rc == WFS_OK && o.nq) rc = observe_launch<R>(h, o, slot);
+        for (int p = 0; p < nplane && rc == WFS_OK; ++p) {
+            int grid = 0;
+            {
+                PassScope ps(h, WFS_PASS_OBSERVE);
+                CK(launch_plane_current<R>(reinterpret_cast<const Cx<R>*>(h->psi), pa[p], h->partials,
+                                           kPlaneCurrentBlocks, nullptr, h->stream, &grid));
+            }
+            PassScope ps(h, WFS_PASS_OTHER);
+            CK(launch_reduce_partials(h->partials, grid, 1, slot + o.nq + p, h->stream));
+        }
         if (rc == WFS_OK) rc = split_steps<R>(h, (i + interval <= nsteps) ? interval : nsteps - i, dt, mass);
     }
     if (rc == WFS_OK && nrec) {
-        std::vector<double> raw(size_t(nrec) * o.nq);
+        std::vector<double> raw(size_t(nrec) * stride);
         cudaError_t e = cudaMemcpyAsync(raw.data(), dser, raw.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
         if (e == cudaSuccess) e = queue_status(h);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -603,12 +664,15 @@ int do_run_split(wfs_handle* h, int nsteps, double dt, double mass, int interval
         if (rc == WFS_OK) rc = take_status(h);
         for (int k = 0; k < nrec && rc == WFS_OK; ++k) {
             double rr[3], rr2[3];
-            finish_obs(h, o, raw.data() + size_t(k) * o.nq, prob_series ? prob_series + size_t(k) * nbox : nullptr, rr, rr2);
+            const double* rk = raw.data() + size_t(k) * stride;
+            finish_obs(h, o, rk, prob_series ? prob_series + size_t(k) * nbox : nullptr, rr, rr2);
             if (loc && loc_series)
                 for (int a = 0; a < 3; ++a) {
                     loc_series[k * 6 + a] = rr[a];
                     loc_series[k * 6 + 3 + a] = rr2[a];
                 }
+            if (flux_series)
+                for (int p = 0; p < nplane; ++p) flux_series[size_t(k) * nplane + p] = rk[o.nq + p] * pscale[p];
         }
     }
     return rc;
@@ -1052,6 +1116,16 @@ int wfs_observe(wfs_handle* h, const wfs_box* boxes, int32_t nbox, const wfs_box
                      : do_observe<float>(h, boxes, nbox, loc, prob_out, r_out, r2_out);
 }
 
+int wfs_run_split_planes(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t interval, const wfs_box* boxes,
+                         int32_t nbox, const wfs_box* loc, const wfs_plane* planes, int32_t nplane, double* prob_series,
+                         double* loc_series, double* flux_series) {
+    if (!h) return dispatch_err(h);
+    return is_dbl(h) ? do_run_split<double>(h, nsteps, dt, mass, interval, boxes, nbox, loc, prob_series, loc_series,
+                                            planes, nplane, flux_series)
+                     : do_run_split<float>(h, nsteps, dt, mass, interval, boxes, nbox, loc, prob_series, loc_series,
+                                           planes, nplane, flux_series);
+}
+
 int wfs_run_split(wfs_handle* h, int32_t nsteps, double dt, double mass, int32_t interval, const wfs_box* boxes, int32_t nbox,
                   const wfs_box* loc, double* prob_series, double* loc_series) {
     if (!h) return dispatch_err(h);
@@ -1128,27 +1202,14 @@ int wfs_split_step_gain(const int32_t n[3], int32_t dtype, double* g_x, double* 
 int wfs_plane_current(wfs_handle* h, const double center[3], const double normal[3], const double size[2],
                       const int32_t count[2], double mass, double* flux_out, void* density_out, int32_t to_device) {
     if (!h) return dispatch_err(h);
-    if (!center || !normal || !size || !count || !flux_out || !(mass > 0)) return set_err(h, WFS_ERR_ARG, "invalid argument");
-    if (count[0] < 3 || count[1] < 3 || (count[0] % 2) == 0 || (count[1] % 2) == 0)
-        return set_err(h, WFS_ERR_ARG, "sample counts must be odd and >= 3 (Simpson)");
+    if (!flux_out) return set_err(h, WFS_ERR_ARG, "null flux output");
     PlaneCurrentArgs a;
-    std::memset(&a, 0, sizeof(a));
-    if (!plane_frame(normal, a.normal, a.right, a.up)) return set_err(h, WFS_ERR_ARG, "degenerate plane normal");
-    for (int k = 0; k < 3; ++k) {
-        a.n[k] = h->n[k];
-        a.dx[k] = h->dx[k];
-        a.center[k] = float(center[k]);
-    }
-    a.sx = count[0];
-    a.sy = count[1];
-    a.mass = mass;
-    const double dW = is_dbl(h) ? size[0] / double(a.sx - 1) : double(float(size[0]) / float(a.sx - 1));
-    const double dH = is_dbl(h) ? size[1] / double(a.sy - 1) : double(float(size[1]) / float(a.sy - 1));
-    a.dWf = float(dW);
-    a.dHf = float(dH);
-    int rc = is_dbl(h) ? to_real<double>(h) : to_real<float>(h);
+    double dW = 0, dH = 0;
+    int rc = fill_plane(h, center, normal, size, count, mass, a, &dW, &dH);
     if (rc) return rc;
-    const int max_blocks = 1024;
+    rc = is_dbl(h) ? to_real<double>(h) : to_real<float>(h);
+    if (rc) return rc;
+    const int max_blocks = kPlaneCurrentBlocks;
     if ((rc = ensure_partials(h, max_blocks))) return rc;
     const size_t dbytes = size_t(a.sx) * a.sy * (is_dbl(h) ? sizeof(double) : sizeof(float));
     void* dens = nullptr;

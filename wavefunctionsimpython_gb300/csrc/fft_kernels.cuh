@@ -86,18 +86,90 @@ __device__ __forceinline__ R simpson_w(int v, int b, int cnt) {
 }
 
 // Observation sums (volume probabilities with Simpson weights, location moments).
-// A thread sums its own elements and a warp its threads in the working precision
-// (short sums); only the sums of warps and, in reduce_partials_kernel, of CTAs are
-// FP64, since GB300's FP64 rate is a small fraction of its FP32 rate. Partials are
-// laid out [CTA][nbox box probabilities, then the 7 location sums].
-//
-// Sums v over the warp in the working precision and stores the sum, as FP64, at
-// scratch[q * 32 + warp]; every lane of the warp must call it.
+// Complex128 sums run in FP64 throughout. Complex64 sums are accumulated by each
+// thread and across the warp as compensated float-float pairs (hi, lo): every add is an
+// error-free transformation (TwoSum) whose rounding error is carried in lo, so the pair
+// holds the sum to about 2^-46 relative, as accurate as an FP64 accumulation of the
+// float32 terms, at FP32 instruction rates (GB300's FP64 rate is about 1/60 of its FP32
+// rate; FP64 adds per element would cost the observation pass more than its HBM
+// traffic). Each warp's pair is converted to FP64 once; CTA and grid sums are FP64 in
+// a fixed order. Partials are laid out [CTA][nbox box probabilities, then the 7
+// location sums]. Location sums carry exact integer offsets from the grid centre
+// (v - N/2); the host multiplies by the spacing in FP64.
 template <typename R>
-__device__ __forceinline__ void warp_sum_to(R v, double* scratch, int q) {
+struct CSum;
+template <>
+struct CSum<double> {
+    double hi = 0.0;
+    __device__ __forceinline__ void add(double v) { hi += v; }
+    __device__ __forceinline__ void merge(const CSum& o) { hi += o.hi; }
+    __device__ __forceinline__ CSum scaled(double k) const { CSum r; r.hi = hi * k; return r; }
+    __device__ __forceinline__ CSum shfl_xor(int m) const {
+        CSum r;
+        r.hi = __shfl_xor_sync(0xffffffffu, hi, m);
+        return r;
+    }
+    __device__ __forceinline__ double value() const { return hi; }
+};
+template <>
+struct CSum<float> {
+    float hi = 0.0f, lo = 0.0f;
+    // TwoSum (Knuth): s + e equals hi + v exactly
+    __device__ __forceinline__ void add(float v) {
+        const float s = __fadd_rn(hi, v);
+        const float vv = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, vv)), __fsub_rn(v, vv));
+        hi = s;
+        lo = __fadd_rn(lo, e);
+    }
+    __device__ __forceinline__ void merge(const CSum& o) {
+        add(o.hi);
+        lo = __fadd_rn(lo, o.lo);
+    }
+    // times k, the product of hi kept exact by its FMA residual (TwoProd)
+    __device__ __forceinline__ CSum scaled(float k) const {
+        CSum r;
+        r.hi = __fmul_rn(hi, k);
+        r.lo = __fmaf_rn(lo, k, __fmaf_rn(hi, k, -r.hi));
+        return r;
+    }
+    __device__ __forceinline__ CSum shfl_xor(int m) const {
+        CSum r;
+        r.hi = __shfl_xor_sync(0xffffffffu, hi, m);
+        r.lo = __shfl_xor_sync(0xffffffffu, lo, m);
+        return r;
+    }
+    __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+};
+
+// |v|^2 with one rounding fewer than x*x + y*y
+__device__ __forceinline__ float abs2(Cx<float> v) { return __fmaf_rn(v.x, v.x, __fmul_rn(v.y, v.y)); }
+__device__ __forceinline__ double abs2(Cx<double> v) { return v.x * v.x + v.y * v.y; }
+
+// Sums v over the warp and stores the sum, as FP64, at scratch[q * 32 + warp]; every
+// lane of the warp must call it.
+template <typename R>
+__device__ __forceinline__ void warp_sum_to(CSum<R> v, double* scratch, int q) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if ((threadIdx.x & 31) == 0) scratch[q * 32 + (threadIdx.x >> 5)] = double(v);
+    for (int m = 16; m > 0; m >>= 1) v.merge(v.shfl_xor(m));
+    if ((threadIdx.x & 31) == 0) scratch[q * 32 + (threadIdx.x >> 5)] = v.value();
+}
+
+// A thread's share of the location sums of one (x, y) row from its sums over z of
+// w = Simpson weight * |psi|^2: s0 = sum w, s1 = sum w kz, s2 = sum w kz^2, with
+// kz = z - nz/2; lxy is the row's Simpson weight (a power of two), kx, ky its offsets.
+// Warp-sums S, S kx, S ky, s1 lxy, S kx^2, S ky^2, s2 lxy into slots q0 .. q0 + 6.
+template <typename R>
+__device__ __forceinline__ void loc_sums_to(const CSum<R>& s0, const CSum<R>& s1, const CSum<R>& s2, R lxy, R kx,
+                                            R ky, double* scratch, int q0) {
+    const CSum<R> S = s0.scaled(lxy);
+    warp_sum_to<R>(S, scratch, q0);
+    warp_sum_to<R>(S.scaled(kx), scratch, q0 + 1);
+    warp_sum_to<R>(S.scaled(ky), scratch, q0 + 2);
+    warp_sum_to<R>(s1.scaled(lxy), scratch, q0 + 3);
+    warp_sum_to<R>(S.scaled(kx * kx), scratch, q0 + 4);
+    warp_sum_to<R>(S.scaled(ky * ky), scratch, q0 + 5);
+    warp_sum_to<R>(s2.scaled(lxy), scratch, q0 + 6);
 }
 // FP64 sums over the warps of quantities [0, nq) into out[blockIdx.x * nq + q]
 // (after a block barrier that follows the warp_sum_to calls).
@@ -430,42 +502,35 @@ __global__ void __launch_bounds__(cmax(P, Q) * W, WFS_MINB_PASS) fft_contig_kern
         const int x = int(row / o.n[1]), y = int(row % o.n[1]);
         R pk[P];
 #pragma unroll
-        for (int k = 0; k < P; ++k) {
-            const Cx<R> v = scale(a2[k], a.scale);
-            pk[k] = own ? v.x * v.x + v.y * v.y : R(0);
-        }
+        for (int k = 0; k < P; ++k) pk[k] = own ? abs2(scale(a2[k], a.scale)) : R(0);
         __syncthreads();  // the transpose scratch is reused for the block sums
         double* scratch = reinterpret_cast<double*>(smem_raw);
 #pragma unroll 1
         for (int b = 0; b < o.nbox; ++b) {
             const ObsBox bx = o.box[b];
             const R wxy = simpson_w<R>(x, bx.b[0], bx.c[0]) * simpson_w<R>(y, bx.b[1], bx.c[1]);
-            R v = R(0);
+            CSum<R> sz;
             if (wxy != R(0)) {
-                R sz = R(0);
 #pragma unroll
-                for (int k = 0; k < P; ++k) sz += simpson_w<R>(t + Q * k, bx.b[2], bx.c[2]) * pk[k];
-                v = wxy * sz;
+                for (int k = 0; k < P; ++k) sz.add(simpson_w<R>(t + Q * k, bx.b[2], bx.c[2]) * pk[k]);
             }
-            warp_sum_to<R>(v, scratch, b);
+            warp_sum_to<R>(sz.scaled(wxy), scratch, b);
         }
         if (o.has_loc) {
-            R s0 = R(0), sz = R(0), szz = R(0);
-#pragma unroll
-            for (int k = 0; k < P; ++k) {
-                const int z = t + Q * k;
-                const R w = simpson_w<R>(z, o.loc.b[2], o.loc.c[2]) * pk[k];
-                const R rz = R(o.dx[2]) * R(z - o.n[2] / 2);
-                s0 += w;
-                sz += w * rz;
-                szz += w * rz * rz;
-            }
+            CSum<R> s0, s1, s2;
             const R lxy = simpson_w<R>(x, o.loc.b[0], o.loc.c[0]) * simpson_w<R>(y, o.loc.b[1], o.loc.c[1]);
-            const R rx = R(o.dx[0]) * R(x - o.n[0] / 2), ry = R(o.dx[1]) * R(y - o.n[1] / 2);
-            const R ls0 = lxy * s0;
-            const R q7[kLocQ] = {ls0, rx * ls0, ry * ls0, lxy * sz, rx * rx * ls0, ry * ry * ls0, lxy * szz};
+            if (lxy != R(0)) {
 #pragma unroll
-            for (int q = 0; q < kLocQ; ++q) warp_sum_to<R>(q7[q], scratch, o.nbox + q);
+                for (int k = 0; k < P; ++k) {
+                    const int z = t + Q * k;
+                    const R w = simpson_w<R>(z, o.loc.b[2], o.loc.c[2]) * pk[k];
+                    const R kz = R(z - o.n[2] / 2);
+                    s0.add(w);
+                    s1.add(w * kz);
+                    s2.add(w * (kz * kz));
+                }
+            }
+            loc_sums_to<R>(s0, s1, s2, lxy, R(x - o.n[0] / 2), R(y - o.n[1] / 2), scratch, o.nbox);
         }
         __syncthreads();
         block_partials(scratch, o.nq, o.partials);

@@ -499,44 +499,35 @@ __global__ void __launch_bounds__(32 * kObsRowsPerCta) observe_real_kernel(const
     const bool own = row < nrows;
     const int x = own ? int(row / o.n[1]) : 0, y = own ? int(row % o.n[1]) : 0;
     const Cx<R>* rp = psi + (own ? row : 0) * o.n[2];
-    auto p2 = [&](int z) {
-        const Cx<R> v = rp[z];
-        return v.x * v.x + v.y * v.y;
-    };
+    auto p2 = [&](int z) { return abs2(rp[z]); };
     // one pass per requested box over the z range where its Simpson weight is nonzero
 #pragma unroll 1
     for (int b = 0; b < o.nbox; ++b) {
         const ObsBox bx = o.box[b];
         const R wxy = own ? simpson_w<R>(x, bx.b[0], bx.c[0]) * simpson_w<R>(y, bx.b[1], bx.c[1]) : R(0);
-        R v = R(0);
+        CSum<R> sz;
         if (wxy != R(0)) {
             const int z0 = bx.b[2] > 0 ? bx.b[2] : 0;
             const int z1 = (bx.b[2] + bx.c[2]) < o.n[2] ? (bx.b[2] + bx.c[2]) : o.n[2];
-            R sz = R(0);
-            for (int z = z0 + lane; z < z1; z += 32) sz += simpson_w<R>(z, bx.b[2], bx.c[2]) * p2(z);
-            v = wxy * sz;
+            for (int z = z0 + lane; z < z1; z += 32) sz.add(simpson_w<R>(z, bx.b[2], bx.c[2]) * p2(z));
         }
-        warp_sum_to<R>(v, scratch, b);
+        warp_sum_to<R>(sz.scaled(wxy), scratch, b);
     }
     if (o.has_loc) {
         const R lxy = own ? simpson_w<R>(x, o.loc.b[0], o.loc.c[0]) * simpson_w<R>(y, o.loc.b[1], o.loc.c[1]) : R(0);
-        R s0 = R(0), sz = R(0), szz = R(0);
+        CSum<R> s0, s1, s2;
         if (lxy != R(0)) {
             const int z0 = o.loc.b[2] > 0 ? o.loc.b[2] : 0;
             const int z1 = (o.loc.b[2] + o.loc.c[2]) < o.n[2] ? (o.loc.b[2] + o.loc.c[2]) : o.n[2];
             for (int z = z0 + lane; z < z1; z += 32) {
                 const R w = simpson_w<R>(z, o.loc.b[2], o.loc.c[2]) * p2(z);
-                const R rz = R(o.dx[2]) * R(z - o.n[2] / 2);
-                s0 += w;
-                sz += w * rz;
-                szz += w * rz * rz;
+                const R kz = R(z - o.n[2] / 2);
+                s0.add(w);
+                s1.add(w * kz);
+                s2.add(w * (kz * kz));
             }
         }
-        const R rx = R(o.dx[0]) * R(x - o.n[0] / 2), ry = R(o.dx[1]) * R(y - o.n[1] / 2);
-        const R ls0 = lxy * s0;
-        const R q7[kLocQ] = {ls0, rx * ls0, ry * ls0, lxy * sz, rx * rx * ls0, ry * ry * ls0, lxy * szz};
-#pragma unroll
-        for (int q = 0; q < kLocQ; ++q) warp_sum_to<R>(q7[q], scratch, o.nbox + q);
+        loc_sums_to<R>(s0, s1, s2, lxy, R(x - o.n[0] / 2), R(y - o.n[1] / 2), scratch, o.nbox);
     }
     __syncthreads();
     block_partials(scratch, o.nq, o.partials);
@@ -577,16 +568,15 @@ cudaError_t launch_reduce_partials(const double* partials, int nblocks, int nq, 
 template <typename R>
 __global__ void __launch_bounds__(256) norm_kernel(const Cx<R>* __restrict__ psi, int64_t count, double* partials, int* flag) {
     __shared__ double scratch[32];
-    R st = R(0);  // per-thread sum in the working precision (a few dozen terms)
+    CSum<R> st;  // compensated per-thread sum
     bool bad = false;
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
-        Cx<R> v = psi[i];
-        R p = v.x * v.x + v.y * v.y;
+        const R p = abs2(psi[i]);
         if (!isfinite(p)) bad = true;
-        st += p;
+        st.add(p);
     }
     if (bad) atomicExch(flag, 1);
-    double s = double(st);
+    double s = st.value();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     if (lane == 0) scratch[warp] = s;

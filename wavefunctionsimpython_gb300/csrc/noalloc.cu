@@ -40,14 +40,16 @@ constexpr int kNoAllocRawSlot = kNoAllocScratchDoubles - 16;   // 16 doubles for
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
-// raw sums -> caller's output: probabilities, then <r>[3] and <r^2>[3]
-__global__ void noalloc_finish_kernel(const double* __restrict__ raw, int nbox, int has_loc, double dv,
-                                      double* __restrict__ out) {
+// raw sums -> caller's output: probabilities, then <r>[3] and <r^2>[3] (the location
+// sums carry integer offsets from the grid centre; the spacing is applied here)
+__global__ void noalloc_finish_kernel(const double* __restrict__ raw, int nbox, int has_loc, double dv, double dx,
+                                      double dy, double dz, double* __restrict__ out) {
     const int i = threadIdx.x;
     if (i < nbox) out[i] = raw[i] * dv;
     if (has_loc && i < 3) {
-        out[nbox + i] = raw[nbox + 1 + i] * dv;
-        out[nbox + 3 + i] = raw[nbox + 4 + i] * dv;
+        const double d = i == 0 ? dx : (i == 1 ? dy : dz);
+        out[nbox + i] = raw[nbox + 1 + i] * d * dv;
+        out[nbox + 3 + i] = raw[nbox + 4 + i] * (d * d) * dv;
     }
 }
 
@@ -169,7 +171,8 @@ extern "C" int wfs_observe_noalloc(const void* psi_device, int32_t dtype, const 
     if (e == cudaSuccess) e = launch_reduce_partials(scratch, grid, o.nq, scratch + kNoAllocRawSlot, s);
     if (e == cudaSuccess) {
         const double dv = o.dx[0] * o.dx[1] * o.dx[2] / 27.0;
-        noalloc_finish_kernel<<<1, 32, 0, s>>>(scratch + kNoAllocRawSlot, nbox, o.has_loc, dv, out_device);
+        noalloc_finish_kernel<<<1, 32, 0, s>>>(scratch + kNoAllocRawSlot, nbox, o.has_loc, dv, o.dx[0], o.dx[1], o.dx[2],
+                                               out_device);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return fail(WFS_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));

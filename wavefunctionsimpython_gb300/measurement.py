@@ -204,14 +204,22 @@ class MeasurementTools:
         return self.__expected_location
 
     def fusable(self) -> bool:
-        """True when every enabled measurement is computed by the fused device loop."""
-        return (len(self.active_plane_currents()) == 0 and len(self.active_volume_probabilities()) <= 8
-                and self.__volumetric is None)
+        """True when every enabled measurement is computed by the fused device loop
+        (volume probabilities, the expected location and plane probability currents)."""
+        return len(self.active_volume_probabilities()) <= 8 and self.__volumetric is None
 
     def observation_request(self):
         boxes = [v.box for v in self.active_volume_probabilities()]
         loc = self.__expected_location.box if self.__expected_location is not None else None
         return boxes, loc
+
+    def plane_request(self):
+        """(center, normal, size, sample_count) of every enabled plane current."""
+        return [(p.center, p.normal, p.size, p.sample_count) for p in self.active_plane_currents()]
+
+    def record_fluxes(self, fluxes):
+        for p, f in zip(self.active_plane_currents(), fluxes):
+            p.append(float(f))
 
     def record(self, probs, er=None, er2=None):
         for v, p in zip(self.active_volume_probabilities(), probs):
