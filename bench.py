@@ -236,8 +236,56 @@ def run_reference(args):
                              "sample": f"{steps} full 256^3 steps of the NumPy/SciPy oracle split step "
                                        f"(scipy.fft, workers={workers})"},
             "e2e": {"value": value, "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    gpu = reference_gpu_path(args)
+    if gpu is not None:
+        line["reference_gpu_path"] = gpu
     print(json.dumps(line))
     return 0
+
+
+def reference_gpu_path(args):
+    """The reference's own GPU path for this workload on this GPU, when its kernels were
+    compiled (oracle/_ref): its kinetic and potential kernels and its packet and potential
+    builders, launched on its own call sequence, with cuFFT (torch.fft, norm="ortho") for
+    the transforms CuPy makes (sources/sim_state.py:641-697). Device-timed full 256^3
+    steps; the P(x > 1) observation the reference makes every 20 steps is included."""
+    try:
+        import torch
+
+        if not torch.cuda.is_available():
+            return None
+        from oracle import ref_gpu
+        from oracle import wfs_oracle as orc
+
+        if not ref_gpu.available():
+            return None
+    except Exception:  # noqa: BLE001 - the extra figure is optional
+        return None
+    torch.cuda.set_device(args.device)
+    sc = orc.config3_double_slit(N, EXTENT)
+    sim = ref_gpu.RefSim(sc.n, sc.extent, False, device=args.device)
+    sim.build_scenario(sc)
+    box = transmitted_box()
+    steps = max(20, min(args.steps, 200))
+    steps -= steps % OBS_INTERVAL
+
+    def run(k):
+        for i in range(k):
+            if i % OBS_INTERVAL == 0:
+                sim.volume_probability(*box)
+            sim.split_step(DT, 1.0, 1, host_sync=True)
+
+    run(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    run(steps)
+    stop.record()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(stop) / steps
+    return {"value": N ** 3 / (ms * 1e-3), "unit": "site-steps/s", "ms_per_step": ms, "steps": steps,
+            "what": "the reference's own CUDA kernels (compiled unchanged) on its call sequence with its "
+                    "per-step host synchronisation, cuFFT via torch.fft for its transforms, one GPU, complex64"}
 
 
 def run_own(args):

@@ -257,8 +257,9 @@ class RefSim:
         fn = _function(build_ref.fatbin_name("potential_operator", self.prec), "potential_operator_kernel")
         _launch(fn, self.grid, self.block, [self.psi, self.V, self.real(dt)])
 
-    def split_step(self, dt, mass=1.0, nsteps=1):
-        """sim_state.py:641-697, nsteps times."""
+    def split_step(self, dt, mass=1.0, nsteps=1, host_sync=False):
+        """sim_state.py:641-697, nsteps times; host_sync adds the stream synchronisation
+        that ends each of the reference's steps (sim_state.py:697)."""
         fft = self.torch.fft
         for _ in range(nsteps):
             self.psi = fft.fftn(self.psi, norm="ortho")
@@ -268,6 +269,8 @@ class RefSim:
             self.psi = fft.fftn(self.psi, norm="ortho")
             self._kinetic(dt, mass)
             self.psi = fft.ifftn(self.psi, norm="ortho")
+            if host_sync:
+                self.torch.cuda.synchronize(self.dev)
 
     def taylor_step(self, dt, mass=1.0, order=10, nsteps=1):
         """sim_state.py:721-752 (single precision: the reference's ping-pong buffers and
