@@ -256,10 +256,13 @@ int wfs_batch_get_psi(wfs_batch* b, int32_t i, void* psi_c64, int32_t to_device)
 int wfs_batch_run(wfs_batch* b, int32_t nsteps, double dt, double mass, int32_t use_graph);
 /* One Simpson volume probability per instance: boxes[i] -> prob_out[i]. */
 int wfs_batch_observe(wfs_batch* b, const wfs_box* boxes, double* prob_out);
-/* Cluster size (1, 2, 4, 8, 16) and radix orientation (0: P >= Q, 1: swapped) of the step kernel. */
+/* Step schedule and radix orientation (0: P >= Q, 1: swapped). cluster 0 (the
+ * default): two passes per step and size class, an x pass and a plane pass that holds
+ * each yz-plane whole in one CTA's shared memory; cluster 1, 2, 4, 8 or 16: one launch
+ * per step, one cluster of that many CTAs per instance, stages through L2. */
 int wfs_batch_set_config(wfs_batch* b, int32_t cluster, int32_t swap);
 /* Times every configuration over `steps` steps and keeps the fastest (psi is restored);
- * ms_out (optional, 10 entries) receives ms per step for cluster {1,2,4,8,16} x swap {0,1},
+ * ms_out (optional, 12 entries) receives ms per step for cluster {0,1,2,4,8,16} x swap {0,1},
  * -1 where a configuration cannot be scheduled. */
 int wfs_batch_autotune(wfs_batch* b, double dt, double mass, int32_t steps, int32_t* cluster_out, int32_t* swap_out,
                        double* ms_out);

@@ -583,12 +583,12 @@ class Batch:
         self._ck(self.lib.wfs_batch_set_config(self.h, int(cluster), int(swap)))
 
     def autotune(self, dt, mass=1.0, steps=5):
-        """Times cluster {1,2,4,8,16} x radix orientation {0,1}; keeps the fastest.
-        Returns (cluster, swap, table of ms per step)."""
+        """Times the cluster setting {0 (two-pass mode), 1, 2, 4, 8, 16} x radix orientation {0, 1};
+        keeps the fastest. Returns (cluster, swap, table of ms per step)."""
         cl, sw = C.c_int32(), C.c_int32()
-        ms = (C.c_double * 10)()
+        ms = (C.c_double * 12)()
         self._ck(self.lib.wfs_batch_autotune(self.h, float(dt), float(mass), int(steps), C.byref(cl), C.byref(sw), ms))
-        table = {(c, s): ms[s * 5 + k] for s in (0, 1) for k, c in enumerate((1, 2, 4, 8, 16))}
+        table = {(c, s): ms[s * 6 + k] for s in (0, 1) for k, c in enumerate((0, 1, 2, 4, 8, 16))}
         return cl.value, sw.value, table
 
     def launch_count(self) -> int:

@@ -11,6 +11,16 @@
 // the uneven sizes. Launches of a run are captured in a CUDA graph and
 // replayed. The cluster size and the radix orientation of every size class
 // are chosen by timing (wfs_batch_autotune).
+//
+// Two-pass mode (cluster setting 0, the default): each step is, per size class,
+//   an x pass X[Fx K Fx^-1] with one (instance, column tile) per CTA, then
+//   a plane pass with one yz-plane per CTA held whole in shared memory
+//   (an L = 96 plane is 72 KB): Y[Fy^-1] -> Z[Fz^-1 E Fz] -> Y[Fy] there,
+// so psi is read and written once per pass and E once per step (40 B/site-step)
+// with no cluster barriers and no stage data in L2. The one-launch cluster mode
+// reads less in principle (24 B/site-step) but the 16 96^3 instances of the sweep
+// run together and their live stage data overflows L2. Entering and leaving the
+// frequency-space representation use the cluster programs in both modes.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -40,6 +50,9 @@ enum Prog { PROG_ENTER = 0, PROG_STEP_HALF = 1, PROG_STEP_FULL = 2, PROG_FINISH 
 
 template <bool SWAP, int L>
 struct BPlan {
+    // (P, Q): the plan the kernels run; (TP, TQ): the plan of the axis table (two_stage_roots),
+    // whose row blocks are addressed by it
+    static constexpr int TP = PlanOf<L>::P, TQ = PlanOf<L>::Q;
     static constexpr int P = SWAP ? PlanOf<L>::Q : PlanOf<L>::P;
     static constexpr int Q = SWAP ? PlanOf<L>::P : PlanOf<L>::Q;
     static constexpr int T = cmax(P, Q);
@@ -48,7 +61,7 @@ struct BPlan {
 };
 
 // x pass over one instance: pencils along x (row stride L^2), W columns per tile.
-template <int P, int Q, int W>
+template <int P, int Q, int W, int TP, int TQ>
 __device__ __forceinline__ void x_kin_tile(const InstDesc& in, int tile, const Cx<float>* k3, Cx<float>* sm, int tid) {
     constexpr int T = cmax(P, Q);
     const int L = in.L;
@@ -66,7 +79,7 @@ __device__ __forceinline__ void x_kin_tile(const InstDesc& in, int tile, const C
     auto sf = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
     auto si = [&](int k2, int n1) { return (k2 * Q + n1) * W + c; };
     const int tt = in_block ? t : T;
-    two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, P, Q>(in.tw), tt, sf);
+    two_stage<P, Q, -1, TW_ROW>(a1, a2, sm, tw_rows<P, Q, TP, TQ>(in.tw), tt, sf);
     if (tt < Q) {
         Cx<float> cf = mk<float>(0.f, 0.f);
         if (active) cf = scale(cmul(k3[L + col / L], k3[2 * L + col % L]), 1.0f / float(L));
@@ -74,7 +87,7 @@ __device__ __forceinline__ void x_kin_tile(const InstDesc& in, int tile, const C
         for (int k = 0; k < P; ++k) a2[k] = cmul(a2[k], cmul(k3[t + Q * k], cf));
     }
     __syncthreads();
-    two_stage<Q, P, +1, TW_ROW>(a2, a1, sm, tw_rows<Q, P, P, Q>(in.tw), tt, si);
+    two_stage<Q, P, +1, TW_ROW>(a2, a1, sm, tw_rows<Q, P, TP, TQ>(in.tw), tt, si);
     if (active && t < P) {
 #pragma unroll
         for (int i = 0; i < Q; ++i) st_l2<float>(base + int64_t(t + P * i) * plane, a1[i]);
@@ -123,7 +136,8 @@ __device__ __forceinline__ void run_prog(const InstDesc& in, int prog, int rank,
         constexpr int SIGN = decltype(SIGNc)::value;
         for (int tile = rank; tile < ntile_y; tile += CL) {
             const int p = tile / ntile_yp, tc = tile % ntile_yp;
-            plane_y_tile<float, B::P, B::Q, B::WS, SIGN>(in.psi + int64_t(p) * plane, L, tc, in.tw, sy, sm, tid, 0);
+            plane_y_tile<float, B::P, B::Q, B::WS, SIGN, TW_ROW, B::TP, B::TQ>(in.psi + int64_t(p) * plane, L, tc, in.tw,
+                                                                              sy, sm, tid, 0);
             __syncthreads();
         }
     };
@@ -138,7 +152,7 @@ __device__ __forceinline__ void run_prog(const InstDesc& in, int prog, int rank,
     }
     const Cx<float>* k3 = in.kin + ((prog == PROG_STEP_FULL) ? 3 * L : 0);
     for (int tile = rank; tile < ntile_x; tile += CL) {
-        x_kin_tile<B::P, B::Q, B::WS>(in, tile, k3, sm, tid);
+        x_kin_tile<B::P, B::Q, B::WS, B::TP, B::TQ>(in, tile, k3, sm, tid);
         __syncthreads();
     }
     sync();
@@ -189,6 +203,120 @@ __global__ void __launch_bounds__(kBatchThreads, WFS_MINB_BATCH) batch_kernel(co
     }
 }
 
+// ---- two-pass mode ---------------------------------------------------------------------
+// x pass: CTA (tile, j) transforms the column tile `tile` of instance ids[j].
+template <bool SWAP, int L>
+__global__ void __launch_bounds__(kBatchThreads) batch_x_kernel(const InstDesc* __restrict__ insts,
+                                                                 const int* __restrict__ ids, int full) {
+    using B = BPlan<SWAP, L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Cx<float>* sm = reinterpret_cast<Cx<float>*>(smem_raw);
+    const InstDesc in = insts[ids[blockIdx.y]];
+    const Cx<float>* k3 = in.kin + (full ? 3 * L : 0);
+    x_kin_tile<B::P, B::Q, B::WS, B::TP, B::TQ>(in, int(blockIdx.x), k3, sm, threadIdx.x);
+}
+
+// One y tile of a plane held in shared memory (ps, row stride L): the transform of
+// plane_y_tile with its loads and stores in shared memory.
+template <int L, int P, int Q, int W, int SIGN, int TP, int TQ>
+__device__ __forceinline__ void smem_y_tile(Cx<float>* ps, int tile, const Cx<float>* tw, float sc, Cx<float>* sm,
+                                            int tid) {
+    constexpr int T = cmax(P, Q);
+    const bool in_block = tid < T * W;
+    const int c = tid % W, t = tid / W;
+    const int col = tile * W + c;
+    const bool active = in_block && col < L;
+    Cx<float> a1[Q], a2[P];
+    if (t < P) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) a1[i] = active ? ps[(t + P * i) * L + col] : mk<float>(0.f, 0.f);
+    }
+    auto sidx = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
+    two_stage<P, Q, SIGN, TW_ROW>(a1, a2, sm, tw_rows<P, Q, TP, TQ>(tw), in_block ? t : T, sidx);
+    if (active && t < Q) {
+#pragma unroll
+        for (int k = 0; k < P; ++k) ps[(t + Q * k) * L + col] = scale(a2[k], sc);
+    }
+}
+
+// W rows of a plane held in shared memory: Fz^-1, times e (from global), Fz, as plane_z_tile.
+template <int L, int P, int Q, int W>
+__device__ __forceinline__ void smem_z_tile(Cx<float>* ps, const Cx<float>* eplane, int tile, const Cx<float>* tw,
+                                            float sc, Cx<float>* sm, int tid) {
+    constexpr int T = cmax(P, Q);
+    constexpr int RS = cmax(Q * (P + 1), P * (Q + 1));
+    const bool in_block = tid < T * W;
+    const int t = tid % T, r = tid / T;
+    const int row = tile * W + r;
+    const bool active = in_block && row < L;
+    Cx<float>* rp = ps + row * L;
+    const Cx<float>* ep = eplane + int64_t(row) * L;
+    Cx<float> a1[Q], a2[P];
+    if (t < P) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) a1[i] = active ? rp[t + P * i] : mk<float>(0.f, 0.f);
+    }
+    auto sidx_f = [&](int k2, int n1) { return r * RS + k2 * (P + 1) + n1; };
+    auto sidx_i = [&](int k2, int n1) { return r * RS + k2 * (Q + 1) + n1; };
+    const int tt = in_block ? t : T;
+    two_stage<P, Q, +1, TW_ANGLE>(a1, a2, sm, tw, tt, sidx_f);
+    if (tt < Q) {
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            Cx<float> e = active ? ld_stream<float>(ep + t + Q * k) : mk<float>(0.f, 0.f);
+            a2[k] = cmul(a2[k], scale(e, sc));
+        }
+    }
+    __syncthreads();
+    two_stage<Q, P, -1, TW_ANGLE>(a2, a1, sm, tw, tt, sidx_i);
+    if (active && t < P) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) rp[t + P * i] = a1[i];
+    }
+}
+
+template <bool SWAP, int L>
+struct PlaneSmem {
+    using B = BPlan<SWAP, L>;
+    static constexpr int RS = cmax(B::Q * (B::P + 1), B::P * (B::Q + 1));
+    static constexpr int kTile = cmax(L * B::WS, B::WC * RS);  // transpose buffer (complex)
+    static constexpr size_t bytes = sizeof(Cx<float>) * (size_t(L) * L + kTile);
+};
+
+// plane pass: CTA (x, j) takes yz-plane x of instance ids[j] into shared memory, applies
+// Y[Fy^-1] Z[Fz^-1 E Fz] Y[Fy] there and writes it back.
+template <bool SWAP, int L>
+__global__ void __launch_bounds__(kBatchThreads) batch_plane_kernel(const InstDesc* __restrict__ insts,
+                                                                     const int* __restrict__ ids) {
+    using B = BPlan<SWAP, L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Cx<float>* ps = reinterpret_cast<Cx<float>*>(smem_raw);
+    Cx<float>* sm = ps + L * L;
+    const InstDesc in = insts[ids[blockIdx.y]];
+    const int tid = threadIdx.x;
+    const int64_t off = int64_t(blockIdx.x) * L * L;
+    const float4* g4 = reinterpret_cast<const float4*>(in.psi + off);
+    float4* s4 = reinterpret_cast<float4*>(ps);
+    for (int i = tid; i < L * L / 2; i += kBatchThreads) s4[i] = __ldcs(g4 + i);
+    __syncthreads();
+    constexpr int ntile_y = (L + B::WS - 1) / B::WS;
+    constexpr int ntile_z = (L + B::WC - 1) / B::WC;
+    for (int tile = 0; tile < ntile_y; ++tile) {
+        smem_y_tile<L, B::P, B::Q, B::WS, +1, B::TP, B::TQ>(ps, tile, in.tw, in.sy, sm, tid);
+        __syncthreads();
+    }
+    for (int tile = 0; tile < ntile_z; ++tile) {
+        smem_z_tile<L, B::P, B::Q, B::WC>(ps, in.ephase + off, tile, in.tw, 1.0f / float(L), sm, tid);
+        __syncthreads();
+    }
+    for (int tile = 0; tile < ntile_y; ++tile) {
+        smem_y_tile<L, B::P, B::Q, B::WS, -1, B::TP, B::TQ>(ps, tile, in.tw, in.sy, sm, tid);
+        __syncthreads();
+    }
+    float4* d4 = reinterpret_cast<float4*>(in.psi + off);
+    for (int i = tid; i < L * L / 2; i += kBatchThreads) __stcs(d4 + i, s4[i]);
+}
+
 bool batch_size_supported(int L) { return L == 32 || L == 48 || L == 64 || L == 96 || L == 128; }
 
 std::map<std::string, std::pair<int, int>> g_tuned;   // size signature -> (cluster, swap)
@@ -214,12 +342,17 @@ struct wfs_batch {
     std::map<int, int64_t> tw_off;
     InstDesc* dinst;
     int* dorder;
+    std::vector<std::pair<int, std::pair<int, int>>> classes;  // (L, (offset into dclass, count))
+    int* dclass;                  // instance ids grouped by size class
+    std::vector<cudaStream_t> side;   // one stream per size class after the first (two-pass mode)
+    std::vector<cudaEvent_t> ev;      // fork event, then one join event per side stream
     double kin_dt, kin_mass, e_dt;
     bool e_valid;
     int rep;                      // 0 real, 2 H, 3 pending
     int cluster, swap;
     cudaGraphExec_t graph;
     int graph_steps, graph_first, graph_cluster, graph_swap;
+    int64_t graph_launches;
     double* partials;
     size_t partials_cap;
     double* dres;
@@ -259,6 +392,80 @@ cudaError_t launch_batch(wfs_batch* b, int prog, int cluster, int swap) {
     return cudaLaunchKernelEx(&cfg, batch_kernel<false>, (const InstDesc*)b->dinst, (const int*)b->dorder, prog);
 }
 
+template <bool SWAP, int L>
+cudaError_t launch_two_pass_class(wfs_batch* b, int full, const int* ids, int count, cudaStream_t st) {
+    using B = BPlan<SWAP, L>;
+    const int64_t plane = int64_t(L) * L;
+    const size_t xs = sizeof(Cx<float>) * size_t(L) * B::WS;
+    batch_x_kernel<SWAP, L><<<dim3(unsigned((plane + B::WS - 1) / B::WS), unsigned(count)), kBatchThreads, xs,
+                              st>>>((const InstDesc*)b->dinst, ids, full);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    batch_plane_kernel<SWAP, L><<<dim3(unsigned(L), unsigned(count)), kBatchThreads, PlaneSmem<SWAP, L>::bytes,
+                                  st>>>((const InstDesc*)b->dinst, ids);
+    b->launches += 2;
+    return cudaGetLastError();
+}
+
+// One step in two-pass mode: x pass and plane pass of every size class. Launched eagerly,
+// the largest class runs on the batch's stream and every other class on a side stream
+// forked from it and joined back, so the classes share the GPU (0.539 against 0.559 ms
+// per step for the 256-instance sweep). In a captured graph the classes stay in one
+// stream: replayed as parallel branches the same step took 0.583 ms.
+cudaError_t launch_two_pass(wfs_batch* b, int prog, int swap) {
+    const int full = prog == PROG_STEP_FULL;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(b->stream, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusNone;
+    const bool branches = cap == cudaStreamCaptureStatusNone;
+    const size_t nside = (branches && b->classes.size() > 1) ? b->classes.size() - 1 : 0;
+    cudaError_t e = cudaSuccess;
+    if (nside) {
+        e = cudaEventRecord(b->ev[0], b->stream);
+        for (size_t k = 0; k < nside && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->side[k], b->ev[0], 0);
+    }
+    for (size_t k = 0; k < b->classes.size() && e == cudaSuccess; ++k) {
+        const auto& c = b->classes[k];
+        const int* ids = b->dclass + c.second.first;
+        const int count = c.second.second;
+        cudaStream_t st = (k == 0 || !nside) ? b->stream : b->side[k - 1];
+        e = cudaErrorInvalidValue;
+#define WFS_BCASE(L_)                                                                                  \
+    case L_:                                                                                           \
+        e = swap ? launch_two_pass_class<true, L_>(b, full, ids, count, st)                          \
+                 : launch_two_pass_class<false, L_>(b, full, ids, count, st);                         \
+        break;
+        switch (c.first) {
+            WFS_BCASE(32) WFS_BCASE(48) WFS_BCASE(64) WFS_BCASE(96) WFS_BCASE(128)
+            default: break;
+        }
+#undef WFS_BCASE
+        if (e == cudaSuccess && k > 0 && nside) e = cudaEventRecord(b->ev[k], st);
+    }
+    for (size_t k = 1; k <= nside && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->stream, b->ev[k], 0);
+    return e;
+}
+
+// One launch of a step program: two-pass mode for the step programs when the cluster
+// setting is 0, the cluster kernel otherwise (entering and finishing use 8-CTA clusters).
+cudaError_t launch_prog(wfs_batch* b, int prog) {
+    if (b->cluster == 0) {
+        if (prog == PROG_STEP_HALF || prog == PROG_STEP_FULL) return launch_two_pass(b, prog, b->swap);
+        return launch_batch(b, prog, 8, b->swap);
+    }
+    return launch_batch(b, prog, b->cluster, b->swap);
+}
+
+template <bool SWAP, int L>
+cudaError_t set_two_pass_attrs() {
+    using B = BPlan<SWAP, L>;
+    cudaError_t e = cudaFuncSetAttribute(batch_plane_kernel<SWAP, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(PlaneSmem<SWAP, L>::bytes));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(batch_x_kernel<SWAP, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(sizeof(Cx<float>) * L * B::WS));
+    return e;
+}
+
 int set_kernel_attrs() {
     static PerDevice done;
     const int dev = current_device();
@@ -267,6 +474,13 @@ int set_kernel_attrs() {
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBatchSmem)) != cudaSuccess) return 1;
         if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 1;
     }
+    cudaError_t e = cudaSuccess;
+#define WFS_BATTR(L_)                                                   \
+    if (e == cudaSuccess) e = set_two_pass_attrs<false, L_>();          \
+    if (e == cudaSuccess) e = set_two_pass_attrs<true, L_>();
+    WFS_BATTR(32) WFS_BATTR(48) WFS_BATTR(64) WFS_BATTR(96) WFS_BATTR(128)
+#undef WFS_BATTR
+    if (e != cudaSuccess) return 1;
     done.put(dev, 1);
     return 0;
 }
@@ -305,7 +519,7 @@ int ensure_tables(wfs_batch* b, double dt, double mass) {
 int materialize(wfs_batch* b) {
     if (b->rep == 0) return WFS_OK;
     if (b->rep == 3) {  // pending: X[K/2], then Y^-1, Z^-1 to real space
-        BCK(launch_batch(b, PROG_FINISH, b->cluster, b->swap));
+        BCK(launch_prog(b, PROG_FINISH));
     } else {            // H: ENTER's inverse is not a program of its own; run FINISH with K/2 = identity
         return berr(b, WFS_ERR_STATE, "internal: unexpected representation");
     }
@@ -322,12 +536,12 @@ int run_steps(wfs_batch* b, int nsteps, double dt, double mass, int use_graph) {
     int rc = ensure_tables(b, dt, mass);
     if (rc) return rc;
     if (b->rep == 0) {
-        BCK(launch_batch(b, PROG_ENTER, b->cluster, b->swap));
+        BCK(launch_prog(b, PROG_ENTER));
         b->rep = 2;
     }
     const int first = (b->rep == 2) ? PROG_STEP_HALF : PROG_STEP_FULL;
     if (!use_graph) {
-        for (int s = 0; s < nsteps; ++s) BCK(launch_batch(b, s == 0 ? first : PROG_STEP_FULL, b->cluster, b->swap));
+        for (int s = 0; s < nsteps; ++s) BCK(launch_prog(b, s == 0 ? first : PROG_STEP_FULL));
     } else {
         if (!(b->graph && b->graph_steps == nsteps && b->graph_first == first && b->graph_cluster == b->cluster &&
               b->graph_swap == b->swap)) {
@@ -336,7 +550,9 @@ int run_steps(wfs_batch* b, int nsteps, double dt, double mass, int use_graph) {
             cudaGraph_t g;
             BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
             cudaError_t e = cudaSuccess;
-            for (int s = 0; s < nsteps && e == cudaSuccess; ++s) e = launch_batch(b, s == 0 ? first : PROG_STEP_FULL, b->cluster, b->swap);
+            const int64_t l0 = b->launches;
+            for (int s = 0; s < nsteps && e == cudaSuccess; ++s) e = launch_prog(b, s == 0 ? first : PROG_STEP_FULL);
+            const int64_t per_replay = b->launches - l0;
             cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
             if (e != cudaSuccess) return berr(b, WFS_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
             if (e2 != cudaSuccess) return berr(b, WFS_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
@@ -347,10 +563,11 @@ int run_steps(wfs_batch* b, int nsteps, double dt, double mass, int use_graph) {
             b->graph_first = first;
             b->graph_cluster = b->cluster;
             b->graph_swap = b->swap;
-            b->launches -= nsteps;  // counted again at each replay
+            b->graph_launches = per_replay;
+            b->launches -= per_replay;  // counted again at each replay
         }
         BCK(cudaGraphLaunch(b->graph, b->stream));
-        b->launches += nsteps;
+        b->launches += b->graph_launches;
     }
     b->rep = 3;
     return WFS_OK;
@@ -387,13 +604,15 @@ int wfs_batch_create(const wfs_batch_desc* d, wfs_batch** out) {
     b->total = 0;
     b->psi = nullptr; b->V = nullptr; b->ephase = nullptr; b->kin = nullptr; b->tw = nullptr;
     b->dinst = nullptr; b->dorder = nullptr; b->graph = nullptr; b->partials = nullptr; b->dres = nullptr;
+    b->dclass = nullptr;
     b->partials_cap = 0;
     b->kin_dt = b->kin_mass = b->e_dt = std::nan("");
     b->e_valid = false;
     b->rep = 0;
-    b->cluster = 8;
+    b->cluster = 0;
     b->swap = 0;
     b->graph_steps = 0;
+    b->graph_launches = 0;
     b->launches = 0;
     int64_t koff = 0;
     for (int i = 0; i < d->ninst; ++i) {
@@ -453,6 +672,27 @@ int wfs_batch_create(const wfs_batch_desc* d, wfs_batch** out) {
     if (e == cudaSuccess) e = cudaMalloc(&b->dorder, b->ninst * sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(b->dinst, hd.data(), hd.size() * sizeof(InstDesc), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->dorder, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice);
+    // size classes for the two-pass mode, largest first (ord is sorted by size)
+    std::vector<int> cls_ids;
+    for (int k = 0; k < b->ninst; ++k) {
+        const int id = ord[k], L = b->L[id];
+        if (b->classes.empty() || b->classes.back().first != L)
+            b->classes.push_back({L, {int(cls_ids.size()), 0}});
+        cls_ids.push_back(id);
+        b->classes.back().second.second += 1;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->dclass, cls_ids.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(b->dclass, cls_ids.data(), cls_ids.size() * sizeof(int), cudaMemcpyHostToDevice);
+    for (size_t k = 0; k < b->classes.size() && e == cudaSuccess; ++k) {
+        cudaEvent_t ev = nullptr;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) b->ev.push_back(ev);
+        if (e == cudaSuccess && k > 0) {
+            cudaStream_t st = nullptr;
+            e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+            if (e == cudaSuccess) b->side.push_back(st);
+        }
+    }
     if (e != cudaSuccess) return fail(std::string("tables: ") + cudaGetErrorString(e));
     auto it = g_tuned.find(b->sig);
     if (it != g_tuned.end()) {
@@ -468,7 +708,12 @@ int wfs_batch_destroy(wfs_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    void* bufs[] = {b->psi, b->V, b->ephase, b->kin, b->tw, b->dinst, b->dorder, b->partials, b->dres};
+    for (cudaStream_t st : b->side) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
+    for (cudaEvent_t ev : b->ev) cudaEventDestroy(ev);
+    void* bufs[] = {b->psi, b->V, b->ephase, b->kin, b->tw, b->dinst, b->dorder, b->partials, b->dres, b->dclass};
     for (void* p : bufs)
         if (p) cudaFree(p);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -622,8 +867,17 @@ int wfs_batch_observe(wfs_batch* b, const wfs_box* boxes, double* prob_out) {
 
 int wfs_batch_set_config(wfs_batch* b, int32_t cluster, int32_t swap) {
     if (!b) return berr(nullptr, WFS_ERR_ARG, "null batch");
-    if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
-        return berr(b, WFS_ERR_ARG, "cluster must be 1, 2, 4, 8 or 16");
+    if (cluster != 0 && cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
+        return berr(b, WFS_ERR_ARG, "cluster must be 0 (two-pass mode), 1, 2, 4, 8 or 16");
+    if (cluster == 0) {
+        if (b->rep != 0 && (b->cluster != 0 || b->swap != (swap ? 1 : 0))) {
+            int rc = materialize(b);
+            if (rc) return rc;
+        }
+        b->cluster = 0;
+        b->swap = swap ? 1 : 0;
+        return WFS_OK;
+    }
     int ncl = 0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(b->ninst * cluster));
@@ -650,7 +904,7 @@ int wfs_batch_set_config(wfs_batch* b, int32_t cluster, int32_t swap) {
 }
 
 int wfs_batch_autotune(wfs_batch* b, double dt, double mass, int32_t steps, int32_t* cluster_out, int32_t* swap_out,
-                       double* ms_out /* [10]: cluster {1,2,4,8,16} x swap {0,1} */) {
+                       double* ms_out /* [12]: cluster setting {0,1,2,4,8,16} x swap {0,1} */) {
     if (!b) return berr(nullptr, WFS_ERR_ARG, "null batch");
     if (steps < 1) steps = 1;
     std::vector<Cx<float>> saved(b->total);
@@ -658,14 +912,14 @@ int wfs_batch_autotune(wfs_batch* b, double dt, double mass, int32_t steps, int3
     if (rc) return rc;
     BCK(cudaStreamSynchronize(b->stream));
     BCK(cudaMemcpy(saved.data(), b->psi, b->total * sizeof(Cx<float>), cudaMemcpyDeviceToHost));
-    const int cls[5] = {1, 2, 4, 8, 16};
+    const int cls[6] = {0, 1, 2, 4, 8, 16};
     double best = 1e30;
     int bc = b->cluster, bs = b->swap;
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
     for (int si = 0; si < 2; ++si)
-        for (int ci = 0; ci < 5; ++ci) {
+        for (int ci = 0; ci < 6; ++ci) {
             double ms_v = -1.0;
             if (wfs_batch_set_config(b, cls[ci], si) == WFS_OK) {
                 rc = run_steps(b, 2, dt, mass, 0);  // warm-up
@@ -686,7 +940,7 @@ int wfs_batch_autotune(wfs_batch* b, double dt, double mass, int32_t steps, int3
                 rc = materialize(b);
                 if (rc) break;
             }
-            if (ms_out) ms_out[si * 5 + ci] = ms_v;
+            if (ms_out) ms_out[si * 6 + ci] = ms_v;
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

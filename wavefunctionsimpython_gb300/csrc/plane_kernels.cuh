@@ -66,7 +66,8 @@ __device__ __forceinline__ Cx<double> ld_stream<double>(const Cx<double>* p) {
 
 // One y-pencil tile (LY rows x W contiguous z columns) of the plane, in place. tw is the axis
 // table (TWL = TW_ROW) or, with TWL = TW_ROW_SMEM, the plan's row block in shared memory.
-template <typename R, int P, int Q, int W, int SIGN, int TWL = TW_ROW>
+// (TP, TQ) is the plan the axis table was built for; (P, Q) may be its transpose.
+template <typename R, int P, int Q, int W, int SIGN, int TWL = TW_ROW, int TP = P, int TQ = Q>
 __device__ __forceinline__ void plane_y_tile(Cx<R>* plane, int nz, int tile, const Cx<R>* tw, R sc, Cx<R>* sm, int tid,
                                              int nthreads) {
     constexpr int T = cmax(P, Q);
@@ -81,7 +82,7 @@ __device__ __forceinline__ void plane_y_tile(Cx<R>* plane, int nz, int tile, con
         for (int i = 0; i < Q; ++i) a1[i] = active ? ld_l2<R>(base + int64_t(t + P * i) * nz) : mk<R>(R(0), R(0));
     }
     auto sidx = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
-    const Cx<R>* rows = (TWL == TW_ROW) ? tw_rows<P, Q, P, Q>(tw) : tw;
+    const Cx<R>* rows = (TWL == TW_ROW) ? tw_rows<P, Q, TP, TQ>(tw) : tw;
     two_stage<P, Q, SIGN, TWL>(a1, a2, sm, rows, in_block ? t : T, sidx);
     if (active && t < Q) {
 #pragma unroll
