@@ -105,6 +105,51 @@ int wfs_fno_make_input(const void* psi, const void* V, float vscale, const doubl
 /* a_b (complex64 [B][n3]) times s_b (invert = 0) or divided by s_b (invert = 1). */
 int wfs_fno_scale_samples(void* a, const double* a2, int32_t invert, int32_t B, int64_t n3, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Inference forward pass on the kept modes (csrc/fno_fast.cu). Same network and
+ * parameters as above, for N = 64, width C = 32, m = 12 only; every product on BF16
+ * tensor cores with FP32 accumulation and every intermediate stored in BF16 (the
+ * jump's correction is about 1e-2 of psi, so this leaves the jump's error unchanged).
+ * Arrays (32-bit words, each two BF16 values):
+ *   H   [B][16][N^3]             channel pairs (2j, 2j+1)
+ *   SZ  [B][32][N][N][12]        z-spectra of each real channel (re, im), kz < 12
+ *   SY  [24][12][B][32][N]       y-spectra on the kept (ky, kz), x fastest
+ * One pass: lift; then per layer ydft(-1), xmix, ydft(+1) and layer (last: last).
+ * SZ and SY must be 16-byte aligned. */
+
+/* h0 = W0 x + b0 (x: [B][2][N^3] complex64, W0p: BF16 [32][16] zero-padded), and SZ
+ * of h0. */
+int wfs_fno_fast_lift(const void* x, const void* W0p, const float* b0, void* h, void* sz, int32_t B, void* stream);
+
+/* h_out = GELU(W h_in + b + Re F^-1 Z) where SZ holds the z-spectra of the layer's
+ * spectral branch (from ydft +1); SZ is then overwritten with the z-spectra of h_out.
+ * W: BF16 [32][32]. h_out must not alias h_in. */
+int wfs_fno_fast_layer(const void* h_in, void* sz, const void* W, const float* bias, void* h_out, int32_t B,
+                       void* stream);
+
+/* Last layer and both projections: out = Wq2 GELU(Wq1 (W h_in + b + Re F^-1 Z) + bq1)
+ * + bq2 + prior (complex64 [B][N^3]). Wq1: BF16 [64][32]; Wq2p: BF16 [8][64], rows
+ * 2..7 zero. */
+int wfs_fno_fast_last(const void* h_in, const void* sz, const void* W, const float* bias, const void* Wq1,
+                      const float* bq1, const void* Wq2p, const float* bq2, const void* prior, void* out, int32_t B,
+                      void* stream);
+
+/* dir = -1: SZ -> SY, the unitary y DFT onto the 24 kept ky; dir = +1: SY -> SZ, its
+ * inverse from the kept ky (the other ky are zero). */
+int wfs_fno_fast_ydft(const void* src, void* dst, int32_t dir, int32_t B, void* stream);
+
+/* In place on SY: the unitary x DFT onto the 24 kept kx, Z = H R per kept mode (Wi from
+ * wfs_fno_pack_mix_interleaved), and the inverse x DFT. */
+int wfs_fno_fast_xmix(void* sy, const void* Wi, int32_t B, void* stream);
+
+/* BF16 mixing weights with interleaved real and imaginary parts: Wi[mode][2o+s'][2i+s]
+ * is the coefficient of (Re, Im)[s] of input channel i in (Re, Im)[s'] of output o. */
+int wfs_fno_pack_mix_interleaved(const float* R, void* Wi, int32_t C, int32_t nmodes, void* stream);
+
+/* dst (BF16 rows_pad x cols_pad) = src (float32 rows x cols), zero padded. */
+int wfs_fno_to_bf16(const float* src, int32_t rows, int32_t cols, void* dst, int32_t rows_pad, int32_t cols_pad,
+                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

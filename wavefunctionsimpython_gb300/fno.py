@@ -54,6 +54,10 @@ def _ptr(t):
     return None if t is None else C.c_void_p(t.data_ptr())
 
 
+# (N, width, modes, hidden) of the inference kernels in csrc/fno_fast.cu
+FAST_GEOMETRY = (64, 32, 12, 64)
+
+
 class FNO:
     """Network parameters, workspaces and the forward / backward / optimiser steps.
 
@@ -93,6 +97,16 @@ class FNO:
         self.WTbf = [torch.empty_like(w) for w in self.Wbf]
         self.ws = None
         self.ws_batch = 0
+        self.fast_ws = None
+        self.fast_batch = 0
+        self.fast_ok = (cfg.N, cfg.width, cfg.modes, cfg.hidden) == FAST_GEOMETRY
+        if self.fast_ok:
+            bf = dict(dtype=torch.bfloat16, device=self.device)
+            self.fast_w = {"W0": torch.empty((c, 16), **bf), "Wq1": torch.empty((h, c), **bf),
+                           "Wq2": torch.empty((8, h), **bf)}
+            for l in range(cfg.layers):
+                self.fast_w[f"W{l + 1}"] = torch.empty((c, c), **bf)
+            self.fast_mix = [torch.empty((nm, 2 * c, 2 * c), **bf) for _ in range(cfg.layers)]
         self.init_params(seed)
 
     # ---- parameters ---------------------------------------------------------------------------
@@ -158,6 +172,14 @@ class FNO:
         for l in range(self.cfg.layers):
             self._ck(self.lib.wfs_fno_pack_weights(_ptr(self.view(f"R{l + 1}")), _ptr(self.Wbf[l]), _ptr(self.WTbf[l]),
                                                    c, self.cfg.nmodes, self._s()), "pack_weights")
+        if self.fast_ok:
+            for name, dst in self.fast_w.items():
+                rows, cols = self.offsets[name][1]
+                self._ck(self.lib.wfs_fno_to_bf16(_ptr(self.view(name)), rows, cols, _ptr(dst), dst.shape[0],
+                                                  dst.shape[1], self._s()), "to_bf16")
+            for l in range(self.cfg.layers):
+                self._ck(self.lib.wfs_fno_pack_mix_interleaved(_ptr(self.view(f"R{l + 1}")), _ptr(self.fast_mix[l]),
+                                                               c, self.cfg.nmodes, self._s()), "pack_mix")
 
     # ---- workspaces ---------------------------------------------------------------------------
     def workspace(self, B):
@@ -219,6 +241,48 @@ class FNO:
         dst = ws["out"] if out is None else out
         ck(lib.wfs_fno_pointwise(_ptr(ws["q"]), hdim, _ptr(self.view("Wq2")), _ptr(self.view("bq2")), _ptr(prior),
                                  None, _ptr(dst), None, 2, B, n3, 0, s), "projection 2")
+        return dst[:B]
+
+    def fast_workspace(self, B):
+        if self.fast_ws is not None and self.fast_batch >= B:
+            return self.fast_ws
+        torch = self.torch
+        cfg = self.cfg
+        i32 = dict(dtype=torch.int32, device=self.device)
+        self.fast_ws = None
+        self.fast_ws = {"h": [torch.empty((B, cfg.width // 2, cfg.n3), **i32) for _ in range(2)],
+                        "sz": torch.empty((B, cfg.width, cfg.N, cfg.N, cfg.modes), **i32),
+                        "sy": torch.empty((2 * cfg.modes, cfg.modes, B, cfg.width, cfg.N), **i32),
+                        "out": torch.empty((B, cfg.n3), dtype=torch.complex64, device=self.device)}
+        self.fast_batch = B
+        return self.fast_ws
+
+    def forward_fast(self, x, prior, B, out=None):
+        """The same network as forward() for inference, on the kept modes only (csrc/fno_fast.cu):
+        BF16 tensor-core products with FP32 accumulation and BF16 intermediates, the z-DFTs fused
+        into the pointwise layers. Geometry N = 64, width 32, 12 modes, projection width 64."""
+        if not self.fast_ok:
+            raise ValueError(f"forward_fast supports (N, width, modes, hidden) = {FAST_GEOMETRY}")
+        cfg, lib, s, ck = self.cfg, self.lib, self._s(), self._ck
+        ws = self.fast_workspace(B)
+        # the kernels address SY, SZ and H with the B they are given: a smaller batch uses
+        # the leading part of each buffer
+        sz, sy, h, L = ws["sz"], ws["sy"], ws["h"], cfg.layers
+        fw = self.fast_w
+        dst = ws["out"] if out is None else out
+        ck(lib.wfs_fno_fast_lift(_ptr(x), _ptr(fw["W0"]), _ptr(self.view("b0")), _ptr(h[0]), _ptr(sz), B, s), "lift")
+        for l in range(L):
+            ck(lib.wfs_fno_fast_ydft(_ptr(sz), _ptr(sy), -1, B, s), "ydft")
+            ck(lib.wfs_fno_fast_xmix(_ptr(sy), _ptr(self.fast_mix[l]), B, s), "xmix")
+            ck(lib.wfs_fno_fast_ydft(_ptr(sy), _ptr(sz), 1, B, s), "ydft inverse")
+            hin, hout = h[l % 2], h[(l + 1) % 2]
+            if l < L - 1:
+                ck(lib.wfs_fno_fast_layer(_ptr(hin), _ptr(sz), _ptr(fw[f"W{l + 1}"]), _ptr(self.view(f"b{l + 1}")),
+                                          _ptr(hout), B, s), "layer")
+            else:
+                ck(lib.wfs_fno_fast_last(_ptr(hin), _ptr(sz), _ptr(fw[f"W{l + 1}"]), _ptr(self.view(f"b{l + 1}")),
+                                         _ptr(fw["Wq1"]), _ptr(self.view("bq1")), _ptr(fw["Wq2"]),
+                                         _ptr(self.view("bq2")), _ptr(prior), _ptr(dst), B, s), "last")
         return dst[:B]
 
     def _wgrad(self, g, cout, x, cin, name_w, B):
@@ -491,9 +555,10 @@ def train(model: FNO, data, batch, steps, lr, warmup=50, log_every=0, time_budge
     return {"steps": done, "seconds": time.perf_counter() - t0, "history": history, "pairs_seen": done * batch}
 
 
-def evaluate(model: FNO, data, batch):
+def evaluate(model: FNO, data, batch, fast=False):
     """Relative L2 errors of prior + network and of the prior alone against the exact
-    jump, per pair (numpy arrays), on normalised data."""
+    jump, per pair (numpy arrays), on normalised data. fast: the inference kernels
+    (FNO.forward_fast) instead of the training forward."""
     torch = model.torch
     x, prior, target = data
     n = x.shape[0]
@@ -505,7 +570,10 @@ def evaluate(model: FNO, data, batch):
     e_net, e_prior, n_net, n_t = [], [], [], []
     for k in range(0, n, batch):
         B = min(batch, n - k)
-        pred = model.forward(x[k:k + B], prior[k:k + B], B, keep_pre=False)
+        if fast:
+            pred = model.forward_fast(x[k:k + B], prior[k:k + B], B)
+        else:
+            pred = model.forward(x[k:k + B], prior[k:k + B], B, keep_pre=False)
         for src, dst in ((pred, e_net), (prior[k:k + B], e_prior)):
             rc = lib.wfs_fno_sample_norms(_ptr(target[k:k + B]), _ptr(src), cfg.n3, B, _ptr(a2), _ptr(d2), s)
             if rc:
