@@ -496,24 +496,25 @@ def run_batch(args):
     return 0
 
 
-def run_surrogate(args):
-    """FNO surrogate (64^3, width 32, 12 modes, 4 layers, BF16 spectral mixing): trains on
-    pairs from the plain split step, then measures held-out jumps of K = 50 steps against
-    the exact propagator, the acceptance rate at the 1e-2 tolerance, and the effective
-    speedup plain / (surrogate + rejected * plain + verified * plain)."""
+def surrogate_distribution(args, dist, stream):
+    """Trains the FNO surrogate (64^3, width 32, 12 modes, 4 layers) on pairs from the plain
+    split step of one scenario distribution, then measures held-out jumps of K = 50 steps
+    against the exact propagator, the acceptance rate at the 1e-2 tolerance, and the
+    effective speedup plain / (surrogate + rejected * plain + verified * plain). Inference
+    (acceptance and timing) runs the kept-mode BF16 pass (FNO.forward_fast); the training
+    forward's errors on the same seeds are reported beside it."""
     import ctypes
 
     import torch
     from wavefunctionsimpython_gb300 import fno as F
 
-    torch.cuda.set_device(args.device)
-    stream = engine_stream(torch)
-    if args.fno_dist == "inband":
+    if dist == "inband":
         # oscillators whose packets stay inside the 12 kept modes of a 24-Bohr box
         cfg = F.FnoConfig(extent=24.0, prior_steps=1)
         ranges = F.ScenarioRanges(p_wall=0.0, p_ho=1.0, omega=(0.2, 0.8), sigma=(1.0, 2.0), x0=(-3.0, -1.0),
                                   k0=(0.2, 1.0))
     else:
+        # the batched sweep's barriers and oscillators on its 40-Bohr box
         cfg = F.FnoConfig(extent=40.0, prior_steps=2)
         ranges = F.ScenarioRanges()
     G, W, B = 64, 8, 8
@@ -552,18 +553,19 @@ def run_surrogate(args):
 
     # held-out seeds: one random window per scenario
     rng = np.random.default_rng(777)
-    e_net, e_prior, n_err, kinds = [], [], [], []
+    e_net, e_f32, e_prior, n_err = [], [], [], []
     for g in range(args.fno_eval // G):
         held = F.make_dataset(cfg, G * W, W, G, seed=10_000 + g, stream=stream, gen=gen, ranges=ranges)
         rows = torch.tensor([int(rng.integers(W)) * G + i for i in range(G)], device=held[0].device)
         sel = tuple(torch.index_select(t, 0, rows) for t in held[:3])
-        ev = F.evaluate(model, sel, batch=16)
+        ev = F.evaluate(model, sel, batch=G, fast=True)
         e_net.append(ev["err_net"])
         e_prior.append(ev["err_prior"])
         n_err.append(ev["norm_err_net"])
-        kinds += [held[4][r].kind for r in rows.tolist()]
+        e_f32.append(F.evaluate(model, sel, batch=16)["err_net"])
         del held, sel
-    e_net, e_prior, n_err = np.concatenate(e_net), np.concatenate(e_prior), np.concatenate(n_err)
+    e_net, e_f32, e_prior, n_err = (np.concatenate(e_net), np.concatenate(e_f32), np.concatenate(e_prior),
+                                    np.concatenate(n_err))
     acc_net = (e_net <= tol) & (n_err <= tol)
     acc_prior = e_prior <= tol
 
@@ -593,50 +595,50 @@ def run_surrogate(args):
     lib = model.lib
     sp = ctypes.c_void_p(stream.cuda_stream)
     out = torch.empty_like(prior)
-    IB = 16
 
     def infer():
         lib.wfs_fno_sample_norms(F._ptr(psi), None, cfg.n3, G, F._ptr(a2), None, sp)
         lib.wfs_fno_make_input(F._ptr(psi), F._ptr(gen.V), float(cfg.vscale), F._ptr(a2), F._ptr(x), G, cfg.n3, sp)
         lib.wfs_fno_scale_samples(F._ptr(prior), F._ptr(a2), 1, G, cfg.n3, sp)
-        for k in range(0, G, IB):
-            model.forward(x[k:k + IB], prior[k:k + IB], IB, out=out[k:k + IB], keep_pre=False)
+        model.forward_fast(x, prior, G, out=out)
         lib.wfs_fno_scale_samples(F._ptr(out), F._ptr(a2), 0, G, cfg.n3, sp)
         lib.wfs_fno_sample_norms(F._ptr(out), None, cfg.n3, G, F._ptr(a2), None, sp)
 
+    def infer_f32():
+        for k in range(0, G, 16):
+            model.forward(x[k:k + 16], prior[k:k + 16], 16, out=out[k:k + 16], keep_pre=False)
+
     ms_net = timed(infer, 5) / G
+    ms_net_f32 = timed(infer_f32, 3) / G
     rej_net, rej_prior = 1.0 - acc_net.mean(), 1.0 - acc_prior.mean()
     ms_surr = ms_coarse + ms_net
     speed_net = ms_plain / (ms_surr + (rej_net + verify_frac) * ms_plain)
     speed_prior = ms_plain / (ms_coarse + (rej_prior + verify_frac) * ms_plain)
-    peak, peak_kind = load_peaks()
     nm = cfg.nmodes
-    mix_flops = 2 * 4 * nm * cfg.width * cfg.width * 2 * cfg.layers  # fwd, per sample: 4 real MACs per complex
-    line = {"metric": "FNO surrogate effective speedup vs plain split step (K=50 jumps, 64^3 c64)",
-            "value": speed_net, "unit": "x", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16 spectral mixing / f32", "data": "synthetic",
-            "config": {"workload": f"FNO 64^3 width {cfg.width} modes {cfg.modes} layers {cfg.layers}, "
-                                   f"K={cfg.jump_steps}, prior {cfg.prior_steps} coarse steps",
-                       "distribution": args.fno_dist, "extent": cfg.extent, "ranges": ranges.__dict__,
-                       "train_pairs": nchunks * chunk, "batch": B, "lr": args.fno_lr},
-            "training": {"steps": done, "samples_seen": done * B, "seconds": t_train, "gen_seconds": t_gen,
-                         "ms_per_step": 1e3 * t_train / max(1, done), "loss_history": history[-12:]},
-            "held_out": {"seeds": int(e_net.size), "err_net_mean": float(e_net.mean()),
-                         "err_net_median": float(np.median(e_net)), "err_prior_mean": float(e_prior.mean()),
-                         "err_prior_median": float(np.median(e_prior)), "norm_err_net_max": float(n_err.max()),
-                         "accept_net": float(acc_net.mean()), "accept_prior_only": float(acc_prior.mean())},
-            "ms_per_jump_per_sample": {"plain": ms_plain, "coarse_prior": ms_coarse, "network": ms_net},
-            "effective_speedup": {"surrogate": speed_net, "coarse_prior_only": speed_prior,
-                                  "verify_fraction": verify_frac, "tolerance": tol},
-            "network_only_site_jumps_per_s": cfg.n3 / (ms_net * 1e-3),
-            "spectral_mixing": {"tflops_fwd": mix_flops / (ms_net * 1e-3) / 1e12,
-                                "note": "the mixing is a small share of the network's time; see ms_per_jump"}}
+    mix_flops = 2 * 4 * nm * cfg.width * cfg.width * cfg.layers  # fwd, per sample: 4 real MACs per complex MAC
+    res = {"distribution": dist, "extent": cfg.extent, "prior_steps": cfg.prior_steps, "ranges": ranges.__dict__,
+           "train_pairs": nchunks * chunk, "batch": B, "lr": args.fno_lr,
+           "training": {"steps": done, "samples_seen": done * B, "seconds": t_train, "gen_seconds": t_gen,
+                        "ms_per_step": 1e3 * t_train / max(1, done), "loss_history": history[-12:]},
+           "held_out": {"seeds": int(e_net.size), "err_net_mean": float(e_net.mean()),
+                        "err_net_median": float(np.median(e_net)),
+                        "err_net_training_forward_mean": float(e_f32.mean()),
+                        "err_prior_mean": float(e_prior.mean()), "err_prior_median": float(np.median(e_prior)),
+                        "norm_err_net_max": float(n_err.max()), "accept_net": float(acc_net.mean()),
+                        "accept_net_training_forward": float(((e_f32 <= tol) & (n_err <= tol)).mean()),
+                        "accept_prior_only": float(acc_prior.mean())},
+           "ms_per_jump_per_sample": {"plain": ms_plain, "coarse_prior": ms_coarse, "network": ms_net,
+                                      "network_training_forward": ms_net_f32},
+           "effective_speedup": {"surrogate": speed_net, "coarse_prior_only": speed_prior,
+                                 "verify_fraction": verify_frac, "tolerance": tol},
+           "network_only_site_jumps_per_s": cfg.n3 / (ms_net * 1e-3),
+           "spectral_mixing_tflops": mix_flops / (ms_net * 1e-3) / 1e12}
     if not args.no_cpu_baseline:
         # FP64 NumPy oracle for two held-out jumps: accuracy of the exact engine and of the surrogate
         from oracle import wfs_oracle as orc
 
         held = F.make_dataset(cfg, G, 1, G, seed=20_000, stream=stream, gen=gen, ranges=ranges)
-        pred = model.forward(held[0][:2], held[1][:2], 2).cpu().numpy()
+        pred = model.forward_fast(held[0][:2], held[1][:2], 2).cpu().numpy()
         xs, tg = held[0][:2].cpu().numpy(), held[2][:2].cpu().numpy()
         n3 = (cfg.N,) * 3
         dx = orc.delta_x((cfg.extent,) * 3, n3)
@@ -649,9 +651,34 @@ def run_surrogate(args):
             nrm = np.linalg.norm(ex)
             errs.append({"engine_vs_fp64": float(np.linalg.norm(tg[i].reshape(n3) - ex) / nrm),
                          "surrogate_vs_fp64": float(np.linalg.norm(pred[i].reshape(n3) - ex) / nrm)})
-        dt_cpu = (time.perf_counter() - t0) / 2
-        line["fp64_oracle_check"] = errs
-        line["cpu_baseline"] = {"value": 1.0 / dt_cpu, "unit": "jumps/s", "cores": 1, "kind": "port",
+        res["fp64_oracle_check"] = errs
+        res["cpu_seconds_per_jump"] = (time.perf_counter() - t0) / 2
+    del model, gen
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_surrogate(args):
+    """FNO surrogate on the in-band distribution (the headline) and on the batched sweep's
+    distribution (config 5's ranges), one JSON line."""
+    import torch
+
+    torch.cuda.set_device(args.device)
+    stream = engine_stream(torch)
+    dists = ["inband", "sweep"] if args.fno_dist == "both" else [args.fno_dist]
+    res = {d: surrogate_distribution(args, d, stream) for d in dists}
+    head = res[dists[0]]
+    line = {"metric": "FNO surrogate effective speedup vs plain split step (K=50 jumps, 64^3 c64)",
+            "value": head["effective_speedup"]["surrogate"], "unit": "x", "n_gpus": 1, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 tensor-core products, f32 accumulation",
+            "data": "synthetic",
+            "config": {"workload": "FNO 64^3 width 32 modes 12 layers 4, K=50, jump = coarse prior + network",
+                       "headline_distribution": dists[0]},
+            "gpu_launches_per_forward": 17,
+            "distributions": res}
+    if "cpu_seconds_per_jump" in head:
+        line["cpu_baseline"] = {"value": 1.0 / head["cpu_seconds_per_jump"], "unit": "jumps/s", "cores": 1,
+                                "kind": "port",
                                 "sample": "2 held-out K=50 jumps of the FP64 NumPy split step (pocketfft, 1 thread)"}
     print(json.dumps(line))
     return 0
@@ -700,9 +727,9 @@ def main():
                     help="split: the headline 256^3 double slit; taylor: the 128^3 power-series workload; "
                          "batch: the 256-instance uneven sweep; surrogate: train and measure the FNO jump; "
                          "render: headless volume view frames")
-    ap.add_argument("--fno-dist", choices=["inband", "sweep"], default="inband",
-                    help="surrogate scenarios: oscillators inside the kept modes, or the sweep's barriers and "
-                         "oscillators on a 40-Bohr box")
+    ap.add_argument("--fno-dist", choices=["inband", "sweep", "both"], default="both",
+                    help="surrogate scenarios: oscillators inside the kept modes, the sweep's barriers and "
+                         "oscillators on a 40-Bohr box, or both (one line, the in-band run as the headline)")
     ap.add_argument("--fno-train-seconds", type=float, default=240.0)
     ap.add_argument("--fno-pairs", type=int, default=20480)
     ap.add_argument("--fno-eval", type=int, default=2048)

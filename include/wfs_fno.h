@@ -107,48 +107,56 @@ int wfs_fno_scale_samples(void* a, const double* a2, int32_t invert, int32_t B, 
 
 /* ------------------------------------------------------------------------
  * Inference forward pass on the kept modes (csrc/fno_fast.cu). Same network and
- * parameters as above, for N = 64, width C = 32, m = 12 only; every product on BF16
- * tensor cores with FP32 accumulation and every intermediate stored in BF16 (the
- * jump's correction is about 1e-2 of psi, so this leaves the jump's error unchanged).
- * Arrays (32-bit words, each two BF16 values):
+ * parameters as above, for N = 64, width C = 32, m = 12 and projection width 64 only;
+ * every product on BF16 tensor cores with FP32 accumulation and every intermediate
+ * stored in BF16 (a jump's correction is about 1e-2 of psi, so this leaves the jump's
+ * error unchanged). Arrays (32-bit words, each two BF16 values):
  *   H   [B][16][N^3]             channel pairs (2j, 2j+1)
- *   SZ  [B][32][N][N][12]        z-spectra of each real channel (re, im), kz < 12
- *   SY  [24][12][B][32][N]       y-spectra on the kept (ky, kz), x fastest
- * One pass: lift; then per layer ydft(-1), xmix, ydft(+1) and layer (last: last).
- * SZ and SY must be 16-byte aligned. */
+ *   SY  [B][N x][24 ky][12 kz][32]  y- and z-spectra of each real channel on the kept
+ *                                (ky, kz), (re, im)
+ * One pass: lift; then per layer xmix and layer (the last layer: last). Each lift,
+ * layer and last call handles one (sample, x) plane per CTA: the y and z DFTs of the
+ * spectral branch, the pointwise layer and the activation stay on chip. All pointers
+ * 16-byte aligned. */
 
-/* h0 = W0 x + b0 (x: [B][2][N^3] complex64, W0p: BF16 [32][16] zero-padded), and SZ
- * of h0. */
-int wfs_fno_fast_lift(const void* x, const void* W0p, const float* b0, void* h, void* sz, int32_t B, void* stream);
-
-/* h_out = GELU(W h_in + b + Re F^-1 Z) where SZ holds the z-spectra of the layer's
- * spectral branch (from ydft +1); SZ is then overwritten with the z-spectra of h_out.
- * W: BF16 [32][32]. h_out must not alias h_in. */
-int wfs_fno_fast_layer(const void* h_in, void* sz, const void* W, const float* bias, void* h_out, int32_t B,
-                       void* stream);
-
-/* Last layer and both projections: out = Wq2 GELU(Wq1 (W h_in + b + Re F^-1 Z) + bq1)
- * + bq2 + prior (complex64 [B][N^3]). Wq1: BF16 [64][32]; Wq2p: BF16 [8][64], rows
- * 2..7 zero. */
-int wfs_fno_fast_last(const void* h_in, const void* sz, const void* W, const float* bias, const void* Wq1,
-                      const float* bq1, const void* Wq2p, const float* bq2, const void* prior, void* out, int32_t B,
+/* h0 = W0 x + b0 with x = (psi / s_b, V * vscale) (4 real channels), s_b = sqrt(a2[b]
+ * / N^3) (a2 NULL: s_b = 1), psi and V complex64 with sample strides psi_stride and
+ * v_stride (complex values, even); W0p: BF16 [32][16] zero-padded. Writes H and the
+ * kept y/z-spectra SY of h0. */
+int wfs_fno_fast_lift(const void* psi, int64_t psi_stride, const void* V, int64_t v_stride, float vscale,
+                      const double* a2, const void* W0p, const float* b0, void* h, void* sy, int32_t B,
                       void* stream);
 
-/* dir = -1: SZ -> SY, the unitary y DFT onto the 24 kept ky; dir = +1: SY -> SZ, its
- * inverse from the kept ky (the other ky are zero). */
-int wfs_fno_fast_ydft(const void* src, void* dst, int32_t dir, int32_t B, void* stream);
+/* h_out = GELU(W h_in + b + Re F^-1 Z) where SY holds the spectral branch Z (from
+ * xmix); SY is then overwritten with the spectra of h_out. W: BF16 [32][32]. h_out
+ * must not alias h_in. */
+int wfs_fno_fast_layer(const void* h_in, void* sy, const void* W, const float* bias, void* h_out, int32_t B,
+                       void* stream);
+
+/* Last layer and both projections: out = prior + s_b (Wq2 GELU(Wq1 (W h_in + b +
+ * Re F^-1 Z) + bq1) + bq2), prior and out complex64 [B][N^3], s_b as in the lift
+ * (a2 NULL: 1). Wq1: BF16 [64][32]; Wq2p: BF16 [8][64], rows 2..7 zero. out_norm
+ * (optional, B doubles) is incremented by sum |out_b|^2. */
+int wfs_fno_fast_last(const void* h_in, const void* sy, const void* W, const float* bias, const void* Wq1,
+                      const float* bq1, const void* Wq2p, const float* bq2, const void* prior, const double* a2,
+                      void* out, double* out_norm, int32_t B, void* stream);
 
 /* In place on SY: the unitary x DFT onto the 24 kept kx, Z = H R per kept mode (Wi from
  * wfs_fno_pack_mix_interleaved), and the inverse x DFT. */
 int wfs_fno_fast_xmix(void* sy, const void* Wi, int32_t B, void* stream);
 
-/* BF16 mixing weights with interleaved real and imaginary parts: Wi[mode][2o+s'][2i+s]
- * is the coefficient of (Re, Im)[s] of input channel i in (Re, Im)[s'] of output o. */
+/* BF16 mixing weights with interleaved real and imaginary parts, in fragment order (see
+ * wfs_fno_to_bf16): row 2o+s' of mode's block holds the coefficients of (Re, Im)[s] of
+ * input channel i in (Re, Im)[s'] of output o, column k = 2i+s stored at the column d
+ * with frag_src_col(d) = k. */
 int wfs_fno_pack_mix_interleaved(const float* R, void* Wi, int32_t C, int32_t nmodes, void* stream);
 
-/* dst (BF16 rows_pad x cols_pad) = src (float32 rows x cols), zero padded. */
+/* dst (BF16 rows_pad x cols_pad) = src (float32 rows x cols), zero padded. With
+ * frag_order (cols_pad a multiple of 16) the columns of each 16-column block are stored
+ * in mma fragment order: column 4t+e holds source column 2t+e (e < 2) or 8+2t+e-2, so a
+ * lane's B-fragment words for k = 2t, 2t+1 and 8+2t, 9+2t are adjacent (frag_src_col). */
 int wfs_fno_to_bf16(const float* src, int32_t rows, int32_t cols, void* dst, int32_t rows_pad, int32_t cols_pad,
-                    void* stream);
+                    int32_t frag_order, void* stream);
 
 #ifdef __cplusplus
 }

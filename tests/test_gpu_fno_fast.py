@@ -92,67 +92,52 @@ def rel(a, b):
 
 
 def gelu(x):
-    from scipy.special import erf
+    """The kernels' GELU: the tanh form (within 5e-4 of the erf form the network trains with)."""
+    return 0.5 * x * (1.0 + np.tanh(0.7978845608 * (x + 0.044715 * x ** 3)))
 
-    return 0.5 * x * (1.0 + erf(x / math.sqrt(2.0)))
+
+def frag_cols(W):
+    """Columns of each 16-column block in mma fragment order (wfs_fno_to_bf16 with frag_order)."""
+    d = np.arange(W.shape[1])
+    blk, t, e = d & ~15, (d & 15) >> 2, d & 3
+    return W[:, blk + np.where(e < 2, 2 * t + e, 8 + 2 * t + e - 2)]
 
 
 BF16_TOL = 3e-3   # relative L2 of a BF16-stored result against the float64 restatement
 
 
-def test_y_dft_forward_and_inverse(torch):
-    _, F, G = tables()
-    rng = np.random.default_rng(1)
-    B = 3
-    sz, v = rand_words(torch, (B, C, N, N, M), rng)
-    sy = torch.zeros((K, M, B, C, N), dtype=torch.int32, device="cuda")
-    assert lib().wfs_fno_fast_ydft(ptr(sz), ptr(sy), -1, B, stream(torch)) == 0
-    a = v.transpose(0, 1, 2, 4, 3, 5).reshape(B, C, N, M, 2 * N)          # [b][c][x][kz][2y+s]
-    ref = (a @ F).reshape(B, C, N, M, K, 2).transpose(4, 3, 0, 1, 2, 5)    # [ky][kz][b][c][x][2]
-    assert rel(words(sy), ref) < BF16_TOL
-    sy2, v2 = rand_words(torch, (K, M, B, C, N), rng)
-    out = torch.zeros_like(sz)
-    assert lib().wfs_fno_fast_ydft(ptr(sy2), ptr(out), 1, B, stream(torch)) == 0
-    a = v2.transpose(2, 3, 4, 1, 0, 5).reshape(B, C, N, M, 2 * K)         # [b][c][x][kz][2ky+s]
-    ref = (a @ G).reshape(B, C, N, M, N, 2).transpose(0, 1, 2, 4, 3, 5)   # [b][c][x][y][kz][2]
-    assert rel(words(out), ref) < BF16_TOL
+def y_forward(yz):
+    """[B][C][X][Y][KZ][2] z-spectra -> SY [B][X][KY][KZ][C][2] (BF16-stored), as the kernels."""
+    _, F, _ = tables()
+    Bn = yz.shape[0]
+    a = yz.transpose(0, 2, 4, 1, 3, 5).reshape(Bn, N, M, C, 2 * N)       # [b][x][kz][c][2y+s]
+    return bf16(a @ F).reshape(Bn, N, M, C, K, 2).transpose(0, 1, 4, 2, 3, 5)
 
 
-@pytest.mark.parametrize("B", [3, 17])
-def test_x_dft_mixing_inverse(torch, B):
-    """A partial 16-sample chunk (3) and a full chunk plus one (17)."""
-    _, F, G = tables()
-    rng = np.random.default_rng(B)
-    nm = 4 * M ** 3
-    sy, v = rand_words(torch, (K, M, B, C, N), rng)
-    R = (rng.uniform(-1, 1, (nm, C, C, 2)) / C).astype(np.float32)
-    Wi = torch.empty((nm, 2 * C, 2 * C), dtype=torch.bfloat16, device="cuda")
-    Rt = torch.from_numpy(R).cuda()
-    assert lib().wfs_fno_pack_mix_interleaved(ptr(Rt), ptr(Wi), C, nm, stream(torch)) == 0
-    assert lib().wfs_fno_fast_xmix(ptr(sy), ptr(Wi), B, stream(torch)) == 0
-    got = words(sy)
-    # restatement: forward x DFT (BF16 store), mixing per mode (BF16 store), inverse x DFT
-    a = v.reshape(K, M, B, C, 2 * N)                                       # [ky][kz][b][c][2x+s]
-    H = bf16(a @ F).reshape(K, M, B, C, K, 2)                              # [ky][kz][b][i][kx][2]
-    Hc = H[..., 0] + 1j * H[..., 1]
-    Rb = bf16(R[..., 0]) + 1j * bf16(R[..., 1])                            # [mode][i][o]
-    mode = (np.arange(K)[:, None, None] * K + np.arange(K)[None, :, None]) * M + np.arange(M)[None, None, :]
-    Rm = Rb[mode]                                                          # [kx][ky][kz][i][o]
-    Z = np.einsum("yzbik,kyzio->yzbok", Hc, Rm)                            # [ky][kz][b][o][kx]
-    Zi = np.stack([bf16(Z.real), bf16(Z.imag)], -1).reshape(K, M, B, C, 2 * K)
-    ref = (Zi @ G).reshape(K, M, B, C, N, 2)
-    assert rel(got, ref) < BF16_TOL
+def y_inverse(sy):
+    """SY [B][X][KY][KZ][C][2] -> z-spectra [B][C][X][Y][KZ][2] (BF16-stored)."""
+    _, _, G = tables()
+    Bn = sy.shape[0]
+    a = sy.transpose(0, 1, 3, 4, 2, 5).reshape(Bn, N, M, C, 2 * K)       # [b][x][kz][c][2ky+s]
+    return bf16(a @ G).reshape(Bn, N, M, C, N, 2).transpose(0, 3, 1, 4, 2, 5)
 
 
-def zrow_reference(h, sz, W, b, act):
-    """pre = W h + b + Re F_z^-1 (kept kz of sz) per z-row; returns h_out and its z-spectra."""
+def z_forward(h):
+    """h [B][C][X][Y][Z] -> BF16 z-spectra [B][C][X][Y][KZ][2]."""
     tz, _, _ = tables()
+    return bf16(h.reshape(-1, N) @ tz).reshape(h.shape[:4] + (M, 2))
+
+
+def z_inverse(zs):
+    """z-spectra [B][C][X][Y][KZ][2] -> Re F_z^-1 [B][C][X][Y][Z]."""
+    tz, _, _ = tables()
+    return (zs.reshape(-1, 2 * M) @ tz.T).reshape(zs.shape[:4] + (N,))
+
+
+def pointwise(W, h):
+    """W [o][i] times h [B][i][...] (float64)."""
     Bn = h.shape[0]
-    s = np.einsum("zj,bcxyj->bcxyz", tz, sz.reshape(Bn, C, N, N, 2 * M))
-    pre = np.einsum("oi,bixyz->boxyz", bf16(W), h) + b[None, :, None, None, None] + s
-    out = bf16(gelu(pre) if act else pre)
-    spec = np.einsum("bcxyz,zj->bcxyj", out, tz)
-    return out, spec.reshape(Bn, C, N, N, M, 2)
+    return np.matmul(W, h.reshape(Bn, h.shape[1], -1)).reshape((Bn, W.shape[0]) + h.shape[2:])
 
 
 def h_words(torch, rng, B):
@@ -161,49 +146,95 @@ def h_words(torch, rng, B):
     return t, chans
 
 
-def test_layer_kernel(torch):
-    rng = np.random.default_rng(5)
-    B = 2
-    h, hv = h_words(torch, rng, B)
-    sz, szv = rand_words(torch, (B, C, N, N, M), rng, scale=4.0)
-    W = rng.uniform(-1, 1, (C, C)) / math.sqrt(C)
-    bias = rng.uniform(-0.5, 0.5, C).astype(np.float32)
-    Wt = torch.from_numpy(bf16(W).astype(np.float32)).to(torch.bfloat16).cuda()
-    bt = torch.from_numpy(bias).cuda()
-    hout = torch.empty_like(h)
-    assert lib().wfs_fno_fast_layer(ptr(h), ptr(sz), ptr(Wt), ptr(bt), ptr(hout), B, stream(torch)) == 0
-    ref_h, ref_spec = zrow_reference(hv, szv, W, bias.astype(np.float64), True)
-    got_h = words(hout).reshape(B, C // 2, N ** 3, 2).transpose(0, 1, 3, 2).reshape(B, C, N, N, N)
-    assert rel(got_h, ref_h) < BF16_TOL
-    assert rel(words(sz), ref_spec) < BF16_TOL
+def h_values(t):
+    B = t.shape[0]
+    return words(t).reshape(B, C // 2, N ** 3, 2).transpose(0, 1, 3, 2).reshape(B, C, N, N, N)
 
 
-def test_lift_and_last_kernels(torch):
+def bf16_tensor(torch, a):
+    """Row-major BF16 copy on the GPU (NumPy's fancy indexing may return column-major arrays,
+    whose strides torch.from_numpy would keep)."""
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(torch.bfloat16).cuda().contiguous()
+
+
+def f32_tensor(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda().contiguous()
+
+
+@pytest.mark.parametrize("B", [3, 17])
+def test_x_dft_mixing_inverse(torch, B):
+    """A partial 16-sample chunk (3) and a full chunk plus one (17)."""
+    _, F, G = tables()
+    rng = np.random.default_rng(B)
+    nm = 4 * M ** 3
+    sy, v = rand_words(torch, (B, N, K, M, C), rng)
+    R = (rng.uniform(-1, 1, (nm, C, C, 2)) / C).astype(np.float32)
+    Wi = torch.empty((nm, 2 * C, 2 * C), dtype=torch.bfloat16, device="cuda")
+    Rt = f32_tensor(torch, R)   # argument tensors stay referenced until the call returns
+    assert lib().wfs_fno_pack_mix_interleaved(ptr(Rt), ptr(Wi), C, nm, stream(torch)) == 0
+    assert lib().wfs_fno_fast_xmix(ptr(sy), ptr(Wi), B, stream(torch)) == 0
+    got = words(sy)
+    # restatement: forward x DFT (BF16 store), mixing per mode (BF16 store), inverse x DFT
+    a = v.transpose(2, 3, 0, 4, 1, 5).reshape(K, M, B, C, 2 * N)          # [ky][kz][b][c][2x+s]
+    H = bf16(a @ F).reshape(K, M, B, C, K, 2)                              # [ky][kz][b][i][kx][2]
+    Hc = H[..., 0] + 1j * H[..., 1]
+    Rb = bf16(R[..., 0]) + 1j * bf16(R[..., 1])                            # [mode][i][o]
+    mode = (np.arange(K)[:, None, None] * K + np.arange(K)[None, :, None]) * M + np.arange(M)[None, None, :]
+    Z = np.einsum("yzbik,kyzio->yzbok", Hc, Rb[mode])                      # [ky][kz][b][o][kx]
+    Zi = np.stack([bf16(Z.real), bf16(Z.imag)], -1).reshape(K, M, B, C, 2 * K)
+    ref = (Zi @ G).reshape(K, M, B, C, N, 2).transpose(2, 4, 0, 1, 3, 5)  # [b][x][ky][kz][c][2]
+    assert rel(got, ref) < BF16_TOL
+
+
+def test_lift_plane_kernel(torch):
+    """h0 = W0 (psi / s, V vs) + b0 and its kept spectra, from raw psi and V with a2."""
     rng = np.random.default_rng(6)
     B = 2
-    x = (rng.normal(size=(B, 2, N ** 3)) + 1j * rng.normal(size=(B, 2, N ** 3))).astype(np.complex64)
+    psi = (rng.normal(size=(B, N ** 3)) + 1j * rng.normal(size=(B, N ** 3))).astype(np.complex64) * 3
+    V = (rng.normal(size=(B, N ** 3)) + 1j * rng.normal(size=(B, N ** 3))).astype(np.complex64)
+    a2 = np.array([np.sum(np.abs(psi[b].astype(np.complex128)) ** 2) for b in range(B)])
+    vs = 0.25
     W0 = rng.uniform(-0.5, 0.5, (C, 4))
-    b0 = rng.uniform(-0.5, 0.5, C).astype(np.float32)
+    b0 = rng.uniform(-0.5, 0.5, C)
     W0p = np.zeros((C, 16))
     W0p[:, :4] = bf16(W0)
     h = torch.empty((B, C // 2, N ** 3), dtype=torch.int32, device="cuda")
-    sz = torch.empty((B, C, N, N, M), dtype=torch.int32, device="cuda")
-    W0t = torch.from_numpy(W0p.astype(np.float32)).to(torch.bfloat16).cuda()
-    assert lib().wfs_fno_fast_lift(ptr(torch.from_numpy(x).cuda()), ptr(W0t), ptr(torch.from_numpy(b0).cuda()),
-                                   ptr(h), ptr(sz), B, stream(torch)) == 0
-    xc = np.empty((B, 4, N ** 3))
-    xc[:, 0::2], xc[:, 1::2] = bf16(x.real), bf16(x.imag)
-    pre = np.einsum("oi,bin->bon", bf16(W0), xc) + b0[None, :, None]
-    ref_h = bf16(pre).reshape(B, C, N, N, N)
-    tz, _, _ = tables()
-    ref_spec = np.einsum("bcxyz,zj->bcxyj", ref_h, tz).reshape(B, C, N, N, M, 2)
-    got_h = words(h).reshape(B, C // 2, N ** 3, 2).transpose(0, 1, 3, 2).reshape(B, C, N, N, N)
-    assert rel(got_h, ref_h) < BF16_TOL
-    assert rel(words(sz), ref_spec) < BF16_TOL
+    sy = torch.empty((B, N, K, M, C), dtype=torch.int32, device="cuda")
+    args = [torch.from_numpy(psi).cuda(), torch.from_numpy(V).cuda(), torch.from_numpy(a2).cuda(),
+            bf16_tensor(torch, frag_cols(W0p)), f32_tensor(torch, b0)]
+    assert lib().wfs_fno_fast_lift(ptr(args[0]), N ** 3, ptr(args[1]), N ** 3, vs, ptr(args[2]), ptr(args[3]),
+                                   ptr(args[4]), ptr(h), ptr(sy), B, stream(torch)) == 0
+    sb = np.sqrt(a2 / N ** 3).astype(np.float32)
+    xs = np.empty((B, 4, N ** 3))
+    p32 = (psi / sb[:, None].astype(np.complex64)).astype(np.complex64)
+    v32 = (V * np.float32(vs)).astype(np.complex64)
+    xs[:, 0], xs[:, 1], xs[:, 2], xs[:, 3] = bf16(p32.real), bf16(p32.imag), bf16(v32.real), bf16(v32.imag)
+    ref_h = bf16(pointwise(bf16(W0), xs) + b0.astype(np.float32)[None, :, None]).reshape(B, C, N, N, N)
+    assert rel(h_values(h), ref_h) < BF16_TOL
+    assert rel(words(sy), y_forward(z_forward(ref_h))) < BF16_TOL
 
-    # last layer (no activation) and both projections
-    hv = got_h
-    szr, szv = rand_words(torch, (B, C, N, N, M), rng, scale=4.0)
+
+def test_layer_plane_kernel(torch):
+    rng = np.random.default_rng(5)
+    B = 2
+    h, hv = h_words(torch, rng, B)
+    sy, syv = rand_words(torch, (B, N, K, M, C), rng, scale=4.0)
+    W = rng.uniform(-1, 1, (C, C)) / math.sqrt(C)
+    bias = rng.uniform(-0.5, 0.5, C).astype(np.float32)
+    hout = torch.empty_like(h)
+    Wt, bt = bf16_tensor(torch, frag_cols(bf16(W))), f32_tensor(torch, bias)
+    assert lib().wfs_fno_fast_layer(ptr(h), ptr(sy), ptr(Wt), ptr(bt), ptr(hout), B, stream(torch)) == 0
+    pre = pointwise(bf16(W), hv) + bias[None, :, None, None, None] + z_inverse(y_inverse(syv))
+    ref_h = bf16(gelu(pre))
+    assert rel(h_values(hout), ref_h) < BF16_TOL
+    assert rel(words(sy), y_forward(z_forward(ref_h))) < BF16_TOL
+
+
+def test_last_plane_kernel(torch):
+    rng = np.random.default_rng(7)
+    B = 2
+    h, hv = h_words(torch, rng, B)
+    sy, syv = rand_words(torch, (B, N, K, M, C), rng, scale=4.0)
     W = rng.uniform(-1, 1, (C, C)) / math.sqrt(C)
     bias = rng.uniform(-0.5, 0.5, C).astype(np.float32)
     Wq1 = rng.uniform(-1, 1, (64, C)) / math.sqrt(C)
@@ -213,27 +244,28 @@ def test_lift_and_last_kernels(torch):
     Wq2p = np.zeros((8, 64))
     Wq2p[:2] = bf16(Wq2)
     prior = (rng.normal(size=(B, N ** 3)) + 1j * rng.normal(size=(B, N ** 3))).astype(np.complex64)
+    a2 = np.array([2.0e5, 7.0e4])
     out = torch.empty((B, N ** 3), dtype=torch.complex64, device="cuda")
-
-    def bt(a, dt=torch.bfloat16):
-        return torch.from_numpy(np.asarray(a, np.float32)).to(dt).cuda()
-
-    assert lib().wfs_fno_fast_last(ptr(h), ptr(szr), ptr(bt(bf16(W))), ptr(bt(bias, torch.float32)),
-                                   ptr(bt(bf16(Wq1))), ptr(bt(bq1, torch.float32)), ptr(bt(Wq2p)),
-                                   ptr(bt(bq2, torch.float32)), ptr(torch.from_numpy(prior).cuda()), ptr(out), B,
+    onorm = torch.zeros(B, dtype=torch.float64, device="cuda")
+    args = [bf16_tensor(torch, frag_cols(bf16(W))), f32_tensor(torch, bias), bf16_tensor(torch, frag_cols(bf16(Wq1))),
+            f32_tensor(torch, bq1), bf16_tensor(torch, frag_cols(Wq2p)), f32_tensor(torch, bq2),
+            torch.from_numpy(prior).cuda(), torch.from_numpy(a2).cuda()]
+    assert lib().wfs_fno_fast_last(ptr(h), ptr(sy), *[ptr(t) for t in args[:7]], ptr(args[7]), ptr(out), ptr(onorm), B,
                                    stream(torch)) == 0
-    s = np.einsum("zj,bcxyj->bcxyz", tz, szv.reshape(B, C, N, N, 2 * M))
-    hl = bf16(np.einsum("oi,bixyz->boxyz", bf16(W), hv) + bias[None, :, None, None, None] + s)
-    q = bf16(gelu(np.einsum("oi,bixyz->boxyz", bf16(Wq1), hl) + bq1[None, :, None, None, None]))
-    o = np.einsum("oi,bixyz->boxyz", bf16(Wq2), q) + bq2[None, :, None, None, None]
-    ref = (o[:, 0] + 1j * o[:, 1]).reshape(B, -1) + prior
+    hl = bf16(pointwise(bf16(W), hv) + bias[None, :, None, None, None] + z_inverse(y_inverse(syv)))
+    q = bf16(gelu(pointwise(bf16(Wq1), hl) + bq1[None, :, None, None, None]))
+    o = pointwise(bf16(Wq2), q) + bq2[None, :, None, None, None]
+    sb = np.sqrt(a2 / N ** 3)
+    ref = prior + sb[:, None] * (o[:, 0] + 1j * o[:, 1]).reshape(B, -1)
     got = out.cpu().numpy()
     assert rel(got - prior, ref - prior) < BF16_TOL
+    np.testing.assert_allclose(onorm.cpu().numpy(), np.sum(np.abs(got.astype(np.complex128)) ** 2, axis=1), rtol=1e-5)
 
 
 def test_forward_fast_matches_training_forward(torch):
     """A network with every parameter random (the last layer included): the correction of the
-    inference pass against the training forward's (FP32 FFTs and activations, BF16 mixing)."""
+    inference pass against the training forward's (FP32 FFTs and activations, BF16 mixing),
+    and the raw-field jump against the normalised pass."""
     from wavefunctionsimpython_gb300 import fno as F
 
     cfg = F.FnoConfig()
@@ -254,3 +286,18 @@ def test_forward_fast_matches_training_forward(torch):
         r = rel((got - prior).cpu().numpy(), (ref - prior).cpu().numpy())
         print(f"B={B}: correction rel L2 fast vs training forward {r:.2e}")
         assert r < 2e-2
+    # raw fields: psi = s x_0, V = x_1 / vscale, prior_raw = s prior -> out_raw = s out
+    B = 3
+    s = torch.tensor([2.0, 0.5, 3.0], dtype=torch.float64, device="cuda")
+    a2 = s ** 2 * cfg.n3
+    psi = (x[:B, 0] * s[:, None].float()).contiguous()
+    V = (x[:B, 1] / cfg.vscale).contiguous()
+    praw = (prior[:B] * s[:, None].float()).contiguous()
+    onorm = torch.zeros(B, dtype=torch.float64, device="cuda")
+    got_raw = model.jump_fast(psi, V, praw, a2, B, out_norm=onorm).clone()
+    got = model.forward_fast(x[:B].contiguous(), prior[:B].contiguous(), B).clone()
+    torch.cuda.synchronize()
+    p = prior[:B].cpu().numpy()
+    r = rel((got_raw / s[:, None].float()).cpu().numpy() - p, got.cpu().numpy() - p)
+    assert r < 5e-3
+    np.testing.assert_allclose(onorm.cpu().numpy(), (got_raw.abs() ** 2).sum(1).double().cpu().numpy(), rtol=1e-5)

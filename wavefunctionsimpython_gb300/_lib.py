@@ -47,7 +47,7 @@ FNO_EXPORTED = [
     "wfs_fno_fft3", "wfs_fno_gather", "wfs_fno_scatter", "wfs_fno_pack_weights", "wfs_fno_mix",
     "wfs_fno_spectral_weight_grad", "wfs_fno_adam", "wfs_fno_loss", "wfs_fno_sample_norms",
     "wfs_fno_make_input", "wfs_fno_scale_samples", "wfs_fno_fast_lift", "wfs_fno_fast_layer",
-    "wfs_fno_fast_last", "wfs_fno_fast_ydft", "wfs_fno_fast_xmix", "wfs_fno_pack_mix_interleaved",
+    "wfs_fno_fast_last", "wfs_fno_fast_xmix", "wfs_fno_pack_mix_interleaved",
     "wfs_fno_to_bf16",
 ]
 SCHEDULES = {"auto": 0, "axis": 1, "plane": 2}
@@ -198,13 +198,12 @@ def load(path: str | os.PathLike | None = None):
         "wfs_fno_sample_norms": ([vp, vp, i64, i32, vp, vp, vp], C.c_int),
         "wfs_fno_make_input": ([vp, vp, C.c_float, vp, vp, i32, i64, vp], C.c_int),
         "wfs_fno_scale_samples": ([vp, vp, i32, i32, i64, vp], C.c_int),
-        "wfs_fno_fast_lift": ([vp, vp, vp, vp, vp, i32, vp], C.c_int),
+        "wfs_fno_fast_lift": ([vp, i64, vp, i64, C.c_float, vp, vp, vp, vp, vp, i32, vp], C.c_int),
         "wfs_fno_fast_layer": ([vp, vp, vp, vp, vp, i32, vp], C.c_int),
-        "wfs_fno_fast_last": ([vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp], C.c_int),
-        "wfs_fno_fast_ydft": ([vp, vp, i32, i32, vp], C.c_int),
+        "wfs_fno_fast_last": ([vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp], C.c_int),
         "wfs_fno_fast_xmix": ([vp, vp, i32, vp], C.c_int),
         "wfs_fno_pack_mix_interleaved": ([vp, vp, i32, i32, vp], C.c_int),
-        "wfs_fno_to_bf16": ([vp, i32, i32, vp, i32, i32, vp], C.c_int),
+        "wfs_fno_to_bf16": ([vp, i32, i32, vp, i32, i32, i32, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -7,24 +7,23 @@
 // and keep its intermediates in BF16 without moving the jump's error. This file does
 // that, and transforms only what the spectral layers use:
 //
-//   z-row kernel   one CTA per 4 z-rows (256 sites, all 32 channels): the inverse
-//                  z-DFT of the layer's spectral branch (12 kept kz -> 64 z) and the
-//                  pointwise 1x1 layer accumulate into one product, then bias, GELU,
-//                  the BF16 store of h, and the forward z-DFT of h (64 z -> 12 kz) with
-//                  the activations transposed in registers (movmatrix). The lift and
-//                  the last layer with both projections are variants of the same kernel.
-//   y kernels      per (sample, channel, 8 x-columns): the 64 -> 24 kept-ky DFT and back.
+//   plane kernel   one CTA per (sample, x) plane: the inverse y and z DFTs of the
+//                  layer's spectral branch, the pointwise 1x1 layer, bias and GELU, the
+//                  BF16 store of h, and the forward z and y DFTs of the new h onto the
+//                  kept (ky, kz), all on chip; h streams through shared memory by cp.async
+//                  two row groups ahead. The lift (with the input normalisation) and the
+//                  last layer with both projections are variants of the same kernel.
 //   x+mix kernel   per kept (ky, kz) and 16 samples: the 64 -> 24 kept-kx DFT, the
 //                  per-mode complex channel mixing Z = H R, and the 24 -> 64 inverse.
 //
 // Every product is mma.sync m16n8k16 (BF16 operands, FP32 accumulation); the DFT
-// matrices are BF16 constants. Traffic per site and sample for four layers is about
-// 1.3 KB plus the mixing weights (56 MB per layer per 16 samples).
+// matrices are BF16 constants. Per layer a site moves its h in and out (128 B) and its
+// share of the kept spectra four times (about 36 B), plus the mixing weights (56 MB per
+// layer per 16 samples).
 //
 // Layouts (bf16x2 words: two channels, or the real and imaginary part of one value):
-//   H   [B][16][64^3]              channel pairs (2j, 2j+1), as the packed layout
-//   SZ  [B][32][64 x][64 y][12 kz] z-spectra of each real channel
-//   SY  [24 ky][12 kz][B][32][64 x] y-spectra, x fastest (the x+mix kernel's rows)
+//   H   [B][16][64^3]                   channel pairs (2j, 2j+1), as the packed layout
+//   SY  [B][64 x][24 ky][12 kz][32 c]   y- and z-spectra of each real channel, kept modes
 // The kept modes follow include/wfs_fno.h: kx, ky in [0, 12) u [52, 64), kz in [0, 12);
 // mode = (ix * 24 + iy) * 12 + iz. Geometry is fixed: N = 64, width 32, 12 modes.
 #include <cuda_bf16.h>
@@ -47,7 +46,6 @@ constexpr int FC = 32;                 // hidden channels
 constexpr int FM = 12;                 // kept kz
 constexpr int FK = 24;                 // kept kx and ky
 constexpr int64_t FN3 = int64_t(FN) * FN * FN;
-constexpr int ZSLAB = FN * FM;         // words of one (b, c, x) z-spectrum slab
 constexpr int NPK = FK * FM;           // kept (ky, kz) pairs
 constexpr int FWD_LD = 68;             // forward DFT matrix row stride in smem (words)
 constexpr int INV_LD = 28;             // inverse DFT matrix row stride in smem (words)
@@ -60,6 +58,11 @@ struct FastTables {
     uint16_t* tzt;   // [32 j][64 z]   transpose of tz
     uint16_t* fwd;   // [48 j][128 k]  forward 64 -> 24 DFT, k = 2 n + s, j = 2 k' + s'
     uint16_t* inv;   // [128 j][48 k]  inverse 24 -> 64 DFT, k = 2 k' + s, j = 2 n + s'
+    // the same constants as per-lane mma fragments (one 16- or 8-byte load per fragment)
+    uint4* inv_a;    // [group 8][ks 3][lane]       inverse y DFT, rows re/im of the group's y
+    uint4* fwd_a;    // [group 8][mt 3][lane]       forward y DFT, rows re/im of 8 ky', cols the group
+    uint4* tz_a;     // [half 2][mt 2][ks 2][lane]  inverse z DFT over a warp's 32 sites
+    uint2* tzt_b;    // [half 2][kk 2][nt 3][lane]  forward z DFT over a warp's 32 sites
 };
 
 std::mutex g_fast_mu;
@@ -108,21 +111,77 @@ const FastTables* fast_tables() {
             inv[(2 * n + 1) * 48 + 2 * kk] = bf16_bits(sn);
             inv[(2 * n + 1) * 48 + 2 * kk + 1] = bf16_bits(c);
         }
-    const size_t words = tz.size() + tzt.size() + fwd.size() + inv.size();
-    uint16_t* d = nullptr;
-    if (cudaMalloc(&d, words * sizeof(uint16_t)) != cudaSuccess) return nullptr;
-    std::vector<uint16_t> all;
-    all.reserve(words);
-    for (auto* v : {&tz, &tzt, &fwd, &inv}) all.insert(all.end(), v->begin(), v->end());
-    if (cudaMemcpy(d, all.data(), words * sizeof(uint16_t), cudaMemcpyHostToDevice) != cudaSuccess) {
+    // fragments: A tile rows R[0..15] x cols K0..K0+15 of a [.][ld] table; B tile of a
+    // table stored [n][k] (k contiguous), n = N0 + g, k = K0..K0+15
+    auto word = [](const std::vector<uint16_t>& t, int ld, int row, int col) {
+        return uint32_t(t[size_t(row) * ld + col]) | (uint32_t(t[size_t(row) * ld + col + 1]) << 16);
+    };
+    std::vector<uint32_t> frags;
+    auto a_tile = [&](const std::vector<uint16_t>& t, int ld, const int* R, int K0) {
+        for (int lane = 0; lane < 32; ++lane) {
+            const int g = lane >> 2, t4 = lane & 3;
+            frags.push_back(word(t, ld, R[g], K0 + 2 * t4));
+            frags.push_back(word(t, ld, R[g + 8], K0 + 2 * t4));
+            frags.push_back(word(t, ld, R[g], K0 + 8 + 2 * t4));
+            frags.push_back(word(t, ld, R[g + 8], K0 + 8 + 2 * t4));
+        }
+    };
+    auto b_tile = [&](const std::vector<uint16_t>& t, int ld, int N0, int K0) {
+        for (int lane = 0; lane < 32; ++lane) {
+            const int g = lane >> 2, t4 = lane & 3;
+            frags.push_back(word(t, ld, N0 + g, K0 + 2 * t4));
+            frags.push_back(word(t, ld, N0 + g, K0 + 8 + 2 * t4));
+        }
+    };
+    int R[16];
+    const size_t off_inv = frags.size();
+    for (int grp = 0; grp < FN / 8; ++grp)
+        for (int ks = 0; ks < 3; ++ks) {
+            for (int i = 0; i < 8; ++i) R[i] = 2 * (8 * grp + i), R[i + 8] = 2 * (8 * grp + i) + 1;
+            a_tile(inv, 48, R, 16 * ks);
+        }
+    const size_t off_fwd = frags.size();
+    for (int grp = 0; grp < FN / 8; ++grp)
+        for (int mt = 0; mt < 3; ++mt) {
+            for (int i = 0; i < 8; ++i) R[i] = 2 * (8 * mt + i), R[i + 8] = 2 * (8 * mt + i) + 1;
+            a_tile(fwd, 128, R, 16 * grp);
+        }
+    const size_t off_tz = frags.size();
+    for (int half = 0; half < 2; ++half)
+        for (int mt = 0; mt < 2; ++mt)
+            for (int ks = 0; ks < 2; ++ks) {
+                for (int i = 0; i < 16; ++i) R[i] = 32 * half + 16 * mt + i;
+                a_tile(tz, 32, R, 16 * ks);
+            }
+    const size_t off_tzt = frags.size();
+    for (int half = 0; half < 2; ++half)
+        for (int kk = 0; kk < 2; ++kk)
+            for (int nt = 0; nt < 3; ++nt) b_tile(tzt, 64, 8 * nt, 32 * half + 16 * kk);
+    const size_t halfs = tz.size() + tzt.size() + fwd.size() + inv.size();
+    const size_t bytes = halfs * sizeof(uint16_t) + frags.size() * sizeof(uint32_t);
+    unsigned char* d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+    std::vector<unsigned char> all(bytes);
+    size_t o = 0;
+    for (auto* v : {&tz, &tzt, &fwd, &inv}) {
+        std::memcpy(all.data() + o, v->data(), v->size() * sizeof(uint16_t));
+        o += v->size() * sizeof(uint16_t);
+    }
+    std::memcpy(all.data() + o, frags.data(), frags.size() * sizeof(uint32_t));
+    if (cudaMemcpy(d, all.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(d);
         return nullptr;
     }
     FastTables t;
-    t.tz = d;
+    t.tz = reinterpret_cast<uint16_t*>(d);
     t.tzt = t.tz + tz.size();
     t.fwd = t.tzt + tzt.size();
     t.inv = t.fwd + fwd.size();
+    uint32_t* fr = reinterpret_cast<uint32_t*>(d + halfs * sizeof(uint16_t));   // 16-byte aligned: halfs = 16384
+    t.inv_a = reinterpret_cast<uint4*>(fr + off_inv);
+    t.fwd_a = reinterpret_cast<uint4*>(fr + off_fwd);
+    t.tz_a = reinterpret_cast<uint4*>(fr + off_tz);
+    t.tzt_b = reinterpret_cast<uint2*>(fr + off_tzt);
     return &(g_fast[dev] = t);
 }
 
@@ -149,348 +208,408 @@ __device__ __forceinline__ uint32_t trans8(uint32_t x) {
     asm volatile("movmatrix.sync.aligned.m8n8.trans.b16 %0, %1;\n" : "=r"(y) : "r"(x));
     return y;
 }
-__device__ __forceinline__ uint32_t w32(const uint16_t* p, int i) {  // two bf16 at an even index
-    return *reinterpret_cast<const uint32_t*>(p + i);
+// GELU in its tanh form, x/2 (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))) (Hendrycks and
+// Gimpel), on the hardware tanh: within 5e-4 of the erf form the network is trained with,
+// below the BF16 rounding of every stored activation.
+__device__ __forceinline__ float gelu(float x) {
+    const float in = x * fmaf(0.0356774081f, x * x, 0.7978845608f);
+    float t;
+    asm("tanh.approx.f32 %0, %1;\n" : "=f"(t) : "f"(in));
+    const float hx = 0.5f * x;
+    return fmaf(hx, t, hx);
 }
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// 16-column blocks of BF16 weights in fragment order: dst column 4 t + e holds source
+// column 2 t + e (e < 2) or 8 + 2 t + e - 2, so a lane's two B-fragment words (k = 2 t4,
+// 2 t4 + 1 and 8 + 2 t4, 9 + 2 t4) are one 8-byte load.
+__host__ __device__ __forceinline__ int frag_src_col(int d) {
+    const int blk = d & ~15, t = (d & 15) >> 2, e = d & 3;
+    return blk + (e < 2 ? 2 * t + e : 8 + 2 * t + e - 2);
+}
+__device__ __forceinline__ uint2 wfrag(const uint16_t* W, int ld, int n, int ks, int t4) {
+    return *reinterpret_cast<const uint2*>(W + n * ld + 16 * ks + 4 * t4);
+}
 
-struct ZrowArgs {
-    const float2* x;        // lift: network input [B][2][n3] complex64 (4 channels)
-    const uint32_t* h;      // layer / last: H of the previous layer
-    uint32_t* sz;           // SZ: read (layer, last) and written (lift, layer), in place
-    const uint16_t* W;      // pointwise weights bf16 [32][16] (lift, zero padded) or [32][32]
-    const float* bias;      // [32]
-    const uint16_t* Wq1;    // last: [64][32]
-    const float* bq1;       // last: [64]
-    const uint16_t* Wq2;    // last: [8][64], rows 2..7 zero
-    const float* bq2;       // last: [2]
-    const float2* prior;    // last: [B][n3] complex64
-    uint32_t* h_out;        // lift / layer: H of this layer
-    float2* out;            // last: prior + network, [B][n3] complex64
-    const uint16_t* tz;
-    const uint16_t* tzt;
-    int B;
+// ---------------------------------------------------------------------------
+// Plane kernel: one CTA (16 warps) per (sample b, column x) owns the yz-plane of 64 z-rows
+// and walks it in 8 groups of 8 rows. Per group:
+//   1. inverse y DFT of the layer's spectral branch, from the plane's y-spectra (SY, in
+//      shared memory) to the group's z-spectra (zs)
+//   2. per warp (row r = w/2, sites z in [32 (w&1), +32)): the pointwise product W h and
+//      the inverse z-DFT T . zs accumulate into one set of fragments; bias, GELU, the BF16
+//      store of the new h; the forward z-DFT of the new h over the warp's 32 sites
+//   3. the two half-rows' z-spectra are summed into ys, and the forward y DFT over the
+//      group's 8 rows accumulates into the plane's new y-spectra (registers)
+// The group's h arrives in shared memory by cp.async two groups ahead. After the last
+// group the new y-spectra are stored over SY[b][x] (read whole at the start: in place).
+// The lift reads psi and V instead of h and skips step 1; the last layer stops after the
+// projections of step 2.
+// ---------------------------------------------------------------------------
+constexpr int PT = 512;                 // threads per plane CTA
+constexpr int GROWS = 8;                // z-rows per group
+constexpr int NGROUP = FN / GROWS;
+constexpr int SY_KS = FM * FC + 8;      // words per ky' of the plane's y-spectra in smem
+constexpr int ZS_KZ = FC + 8;           // words per kz of a row's z-spectra
+constexpr int ZS_Y = FM * ZS_KZ + 8;    // words per row of the group's z-spectra
+constexpr int HS_P = GROWS * FN + 8;    // words per channel pair of the staged h
+constexpr int SYW = NPK * FC;           // words of one plane's y-spectra in global memory
+
+struct PlaneSmem {
+    uint32_t sy[FK * SY_KS];
+    uint32_t zs[GROWS * ZS_Y];
+    uint32_t ys[GROWS * ZS_Y];
+    float2 red[GROWS][FC][FM];
+    uint32_t hs[2][(FC / 2) * HS_P];
 };
 
-enum { ZROW_LIFT = 0, ZROW_LAYER = 1, ZROW_LAST = 2 };
+struct PlaneArgs {
+    const float2* psi;      // lift: field 0 (psi), sample stride psi_stride (complex values)
+    const float2* V;        // lift: field 1 (V), sample stride v_stride
+    int64_t psi_stride, v_stride;
+    float vscale;           // lift: V is scaled by vscale
+    const double* a2;       // lift: psi / s_b, last: prior + s_b net, s_b = sqrt(a2[b] / n3) (NULL: 1)
+    const uint32_t* h;      // layer / last: H of the previous layer
+    uint32_t* sy;           // SY: read (layer, last), written (lift, layer)
+    const uint16_t* W;      // bf16 [32][16] (lift) or [32][32]
+    const float* bias;
+    const uint16_t* Wq1;    // last: [64][32]
+    const float* bq1;
+    const uint16_t* Wq2;    // last: [8][64], rows 2..7 zero
+    const float* bq2;
+    const float2* prior;    // last: [B][n3]
+    uint32_t* h_out;        // lift / layer
+    float2* out;            // last: [B][n3]
+    double* out_norm;       // last, optional: += sum |out|^2 per sample
+    const uint4* inv_a;
+    const uint4* fwd_a;
+    const uint4* tz_a;
+    const uint2* tzt_b;
+};
 
-// One CTA: sample b, column x, rows y0..y0+3 (y0 = 4 * (blockIdx % 16)). Warp w owns
-// row y0 + w/2 and sites z in [32 (w&1), 32 (w&1) + 32): two 16-site m-tiles.
+enum { PLANE_LIFT = 0, PLANE_LAYER = 1, PLANE_LAST = 2 };
+
+__device__ __forceinline__ void cp16(void* smem, const void* gmem) {
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
 template <int MODE>
-__global__ void __launch_bounds__(256) fno_zrow_kernel(const ZrowArgs a) {
-    __shared__ float2 red[4][FC][FM];      // partial forward z-spectra of the second half-rows
-    __shared__ uint32_t szbuf[FC][4 * FM]; // the CTA's finished z-spectra, per channel
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__global__ void __launch_bounds__(PT, 1) fno_plane_kernel(const PlaneArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PlaneSmem& sm = *reinterpret_cast<PlaneSmem*>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t4 = lane & 3;
-    const int yg = blockIdx.x % 16, xcol = (blockIdx.x / 16) % FN, b = blockIdx.x / (16 * FN);
-    const int r = warp >> 1, half = warp & 1, y = 4 * yg + r, z0 = 32 * half;
-    const int64_t row = (int64_t(xcol) * FN + y) * FN;   // site index of z = 0
-    float d[2][4][4];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) d[mt][nt][q] = 0.f;
+    const int xcol = blockIdx.x % FN, b = blockIdx.x / FN;
+    const int r = warp >> 1, half = warp & 1, z0 = 32 * half;
+    const int64_t plane0 = int64_t(xcol) * FN * FN;                  // site of (x, 0, 0)
+    uint32_t* syg = a.sy + (int64_t(b) * FN + xcol) * SYW;           // SY[b][x]
+    float s_b = 1.0f;
+    if ((MODE == PLANE_LIFT || MODE == PLANE_LAST) && a.a2) s_b = float(sqrt(a.a2[b] / double(FN3)));
 
-    if constexpr (MODE == ZROW_LIFT) {
-        // h0 = W0 x + b0: channels (Re psi, Im psi) in pair 0, (Re V s, Im V s) in pair 1
+    // staging of one group's input: h (16 pairs x 512 sites) or psi and V (2 x 512 values)
+    auto stage = [&](int grp) {
+        if (grp < NGROUP) {
+            const int64_t s0 = plane0 + int64_t(grp) * GROWS * FN;
+            uint32_t* dst = sm.hs[grp & 1];
+            if constexpr (MODE == PLANE_LIFT) {
+                // 2 fields x 512 complex values = 2 x 256 chunks of 16 B
+                const int f = tid >> 8, ch = tid & 255;
+                const float2* src = f == 0 ? a.psi + int64_t(b) * a.psi_stride : a.V + int64_t(b) * a.v_stride;
+                cp16(dst + f * HS_P * 2 + ch * 4, src + s0 + ch * 2);
+            } else {
+                const uint32_t* hb = a.h + int64_t(b) * (FC / 2) * FN3;
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            const int64_t s0 = row + z0 + 16 * mt + g;
-            uint32_t A[4] = {0u, 0u, 0u, 0u};
-            if (t4 < 2) {
-                const float2* xb = a.x + (int64_t(b) * 2 + t4) * FN3;
-                const float2 v0 = xb[s0], v1 = xb[s0 + 8];
-                A[0] = pk(v0.x, v0.y);
-                A[1] = pk(v1.x, v1.y);
+                for (int i = 0; i < 4; ++i) {
+                    const int k = tid + PT * i, pr = k >> 7, ch = k & 127;
+                    cp16(dst + pr * HS_P + ch * 4, hb + int64_t(pr) * FN3 + s0 + ch * 4);
+                }
             }
+        }
+        cp_commit();
+    };
+    if constexpr (MODE != PLANE_LIFT) {
+        for (int k = tid; k < SYW / 4; k += PT) {
+            const int p = (k * 4) / FC, c = (k * 4) % FC;   // p = ky' * 12 + kz
+            cp16(sm.sy + (p / FM) * SY_KS + (p % FM) * FC + c, syg + k * 4);
+        }
+    }
+    stage(0);
+    stage(1);
+
+    float acc[3][3][4];   // new y-spectra: m-tile (8 ky': re rows, im rows) x this warp's 3 n-tiles
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+
+    for (int grp = 0; grp < NGROUP; ++grp) {
+        const int y0 = grp * GROWS;
+        const uint32_t* hs = sm.hs[grp & 1];
+        if constexpr (MODE != PLANE_LIFT) {
+            cp_wait1();
+            __syncthreads();   // sy (first group) and this group's h have landed
+            // 1. inverse y DFT: zs[row][kz][c] = sum_ky' G[y][ky'] SY[ky'][kz][c] (interleaved rows:
+            //    re of y0+g in rows 0-7, im in rows 8-15)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int nt = 3 * warp + j, kz = nt >> 2, c = (nt & 3) * 8 + g;
+                float d[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int ks = 0; ks < 3; ++ks) {
+                    const uint4 f = a.inv_a[(grp * 3 + ks) * 32 + lane];
+                    const uint32_t A[4] = {f.x, f.y, f.z, f.w};
+                    const int ky = 8 * ks + t4;
+                    mma(d, A, sm.sy[ky * SY_KS + kz * FC + c], sm.sy[(ky + 4) * SY_KS + kz * FC + c]);
+                }
+                const int cc = (nt & 3) * 8 + 2 * t4;
+                sm.zs[g * ZS_Y + kz * ZS_KZ + cc] = pk(d[0], d[2]);
+                sm.zs[g * ZS_Y + kz * ZS_KZ + cc + 1] = pk(d[1], d[3]);
+            }
+        } else {
+            cp_wait1();
+        }
+        __syncthreads();   // zs ready (and, for the lift, this group's input)
+
+        // 2. pointwise + inverse z-DFT for this warp's 32 sites
+        const int rowsite = r * FN + z0;   // local site of the warp's first z
+        float d[2][4][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt)
-                mma(d[mt][nt], A, w32(a.W, (nt * 8 + g) * 16 + 2 * t4), w32(a.W, (nt * 8 + g) * 16 + 8 + 2 * t4));
-        }
-    } else {
-        // pointwise term W h
-        const uint32_t* hb = a.h + int64_t(b) * (FC / 2) * FN3;
 #pragma unroll
-        for (int ks = 0; ks < 2; ++ks) {
-            uint32_t Bw[4][2];
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-                Bw[nt][0] = w32(a.W, (nt * 8 + g) * 32 + 16 * ks + 2 * t4);
-                Bw[nt][1] = w32(a.W, (nt * 8 + g) * 32 + 16 * ks + 8 + 2 * t4);
-            }
+                for (int q = 0; q < 4; ++q) d[mt][nt][q] = 0.f;
+        if constexpr (MODE == PLANE_LIFT) {
+            // channels (Re psi / s, Im psi / s) in pair 0, (Re V vs, Im V vs) in pair 1
+            const float sc = t4 == 0 ? 1.0f / s_b : a.vscale;
 #pragma unroll
             for (int mt = 0; mt < 2; ++mt) {
-                const int64_t s0 = row + z0 + 16 * mt + g;
-                const uint32_t* p0 = hb + int64_t(8 * ks + t4) * FN3;
-                const uint32_t* p1 = p0 + 4 * FN3;
-                const uint32_t A[4] = {p0[s0], p0[s0 + 8], p1[s0], p1[s0 + 8]};
+                uint32_t A[4] = {0u, 0u, 0u, 0u};
+                if (t4 < 2) {
+                    const uint32_t* f = hs + t4 * HS_P * 2;   // field t4, two words per value
+                    const int s0 = rowsite + 16 * mt + g;
+                    A[0] = pk(__uint_as_float(f[2 * s0]) * sc, __uint_as_float(f[2 * s0 + 1]) * sc);
+                    A[1] = pk(__uint_as_float(f[2 * s0 + 16]) * sc, __uint_as_float(f[2 * s0 + 17]) * sc);
+                }
 #pragma unroll
-                for (int nt = 0; nt < 4; ++nt) mma(d[mt][nt], A, Bw[nt][0], Bw[nt][1]);
+                for (int nt = 0; nt < 4; ++nt) {
+                    const uint2 w = wfrag(a.W, 16, nt * 8 + g, 0, t4);
+                    mma(d[mt][nt], A, w.x, w.y);
+                }
             }
-        }
-        // spectral term: s_c(z) = sum_j T[z][j] W_c[j], W_c = (re, im) of the 12 kept kz
-        const uint32_t* szb = a.sz + ((int64_t(b) * FC * FN + xcol) * FN + y) * FM;   // channel 0
-        const int64_t cstride = int64_t(FN) * FN * FM;
-#pragma unroll
-        for (int ks = 0; ks < 2; ++ks) {
-            uint32_t At[2][4];
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-                const int zr = z0 + 16 * mt + g;
-                At[mt][0] = w32(a.tz, zr * 32 + 16 * ks + 2 * t4);
-                At[mt][1] = w32(a.tz, (zr + 8) * 32 + 16 * ks + 2 * t4);
-                At[mt][2] = w32(a.tz, zr * 32 + 16 * ks + 8 + 2 * t4);
-                At[mt][3] = w32(a.tz, (zr + 8) * 32 + 16 * ks + 8 + 2 * t4);
-            }
-            const int kz0 = 8 * ks + t4, kz1 = kz0 + 4;
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-                const uint32_t* sc = szb + int64_t(nt * 8 + g) * cstride;
-                const uint32_t b0 = kz0 < FM ? sc[kz0] : 0u;
-                const uint32_t b1 = kz1 < FM ? sc[kz1] : 0u;
-#pragma unroll
-                for (int mt = 0; mt < 2; ++mt) mma(d[mt][nt], At[mt], b0, b1);
-            }
-        }
-    }
-
-    // bias (and GELU for hidden layers)
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        const float c0 = a.bias[nt * 8 + 2 * t4], c1 = a.bias[nt * 8 + 2 * t4 + 1];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            d[mt][nt][0] += c0;
-            d[mt][nt][1] += c1;
-            d[mt][nt][2] += c0;
-            d[mt][nt][3] += c1;
-            if constexpr (MODE == ZROW_LAYER) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) d[mt][nt][q] = gelu(d[mt][nt][q]);
-            }
-        }
-    }
-
-    if constexpr (MODE == ZROW_LAST) {
-        // out = Wq2 GELU(Wq1 h + bq1) + bq2 + prior, chained through the fragments
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            uint32_t A1[2][4];
+        } else {
 #pragma unroll
             for (int ks = 0; ks < 2; ++ks) {
-                A1[ks][0] = pk(d[mt][2 * ks][0], d[mt][2 * ks][1]);
-                A1[ks][1] = pk(d[mt][2 * ks][2], d[mt][2 * ks][3]);
-                A1[ks][2] = pk(d[mt][2 * ks + 1][0], d[mt][2 * ks + 1][1]);
-                A1[ks][3] = pk(d[mt][2 * ks + 1][2], d[mt][2 * ks + 1][3]);
+                uint2 Bw[4];
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) Bw[nt] = wfrag(a.W, 32, nt * 8 + g, ks, t4);
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt) {
+                    const int s0 = rowsite + 16 * mt + g;
+                    const uint32_t* p0 = hs + (8 * ks + t4) * HS_P;
+                    const uint32_t* p1 = p0 + 4 * HS_P;
+                    const uint32_t A[4] = {p0[s0], p0[s0 + 8], p1[s0], p1[s0 + 8]};
+#pragma unroll
+                    for (int nt = 0; nt < 4; ++nt) mma(d[mt][nt], A, Bw[nt].x, Bw[nt].y);
+                }
             }
-            float q[8][4];
+            const uint32_t* zr = sm.zs + r * ZS_Y;
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
+            for (int ks = 0; ks < 2; ++ks) {
+                uint32_t At[2][4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) q[nt][i] = 0.f;
+                for (int mt = 0; mt < 2; ++mt) {
+                    const uint4 f = a.tz_a[((half * 2 + mt) * 2 + ks) * 32 + lane];
+                    At[mt][0] = f.x;
+                    At[mt][1] = f.y;
+                    At[mt][2] = f.z;
+                    At[mt][3] = f.w;
+                }
+                const int kz0 = 8 * ks + t4, kz1 = kz0 + 4;
 #pragma unroll
-                for (int ks = 0; ks < 2; ++ks)
-                    mma(q[nt], A1[ks], w32(a.Wq1, (nt * 8 + g) * 32 + 16 * ks + 2 * t4),
-                        w32(a.Wq1, (nt * 8 + g) * 32 + 16 * ks + 8 + 2 * t4));
-                const float c0 = a.bq1[nt * 8 + 2 * t4], c1 = a.bq1[nt * 8 + 2 * t4 + 1];
-                q[nt][0] = gelu(q[nt][0] + c0);
-                q[nt][1] = gelu(q[nt][1] + c1);
-                q[nt][2] = gelu(q[nt][2] + c0);
-                q[nt][3] = gelu(q[nt][3] + c1);
-            }
-            float o[4] = {0.f, 0.f, 0.f, 0.f};
+                for (int nt = 0; nt < 4; ++nt) {
+                    const int c = nt * 8 + g;
+                    const uint32_t b0 = kz0 < FM ? zr[kz0 * ZS_KZ + c] : 0u;
+                    const uint32_t b1 = kz1 < FM ? zr[kz1 * ZS_KZ + c] : 0u;
 #pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-                const uint32_t A2[4] = {pk(q[2 * ks][0], q[2 * ks][1]), pk(q[2 * ks][2], q[2 * ks][3]),
-                                        pk(q[2 * ks + 1][0], q[2 * ks + 1][1]),
-                                        pk(q[2 * ks + 1][2], q[2 * ks + 1][3])};
-                mma(o, A2, w32(a.Wq2, g * 64 + 16 * ks + 2 * t4), w32(a.Wq2, g * 64 + 16 * ks + 8 + 2 * t4));
-            }
-            if (t4 == 0) {
-                const int64_t s0 = int64_t(b) * FN3 + row + z0 + 16 * mt + g;
-                const float2 p0 = a.prior[s0], p1 = a.prior[s0 + 8];
-                a.out[s0] = make_float2(o[0] + a.bq2[0] + p0.x, o[1] + a.bq2[1] + p0.y);
-                a.out[s0 + 8] = make_float2(o[2] + a.bq2[0] + p1.x, o[3] + a.bq2[1] + p1.y);
-            }
-        }
-        return;
-    } else {
-        // store h (BF16 channel pairs) and keep the packed fragments for the z-DFT
-        uint32_t P[2][4][2];
-        uint32_t* hb = a.h_out + int64_t(b) * (FC / 2) * FN3;
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            const int64_t s0 = row + z0 + 16 * mt + g;
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-                P[mt][nt][0] = pk(d[mt][nt][0], d[mt][nt][1]);
-                P[mt][nt][1] = pk(d[mt][nt][2], d[mt][nt][3]);
-                uint32_t* hp = hb + int64_t(nt * 4 + t4) * FN3;
-                hp[s0] = P[mt][nt][0];
-                hp[s0 + 8] = P[mt][nt][1];
+                    for (int mt = 0; mt < 2; ++mt) mma(d[mt][nt], At[mt], b0, b1);
+                }
             }
         }
-        // forward z-DFT of this half-row: Y[c][j] = sum_z h[z][c] T[z][j]; the A operand
-        // (channels x sites) is the transpose of the fragments above
-        float e[2][3][4];
 #pragma unroll
-        for (int qq = 0; qq < 2; ++qq)
+        for (int nt = 0; nt < 4; ++nt) {
+            const float c0 = a.bias[nt * 8 + 2 * t4], c1 = a.bias[nt * 8 + 2 * t4 + 1];
 #pragma unroll
-            for (int nt = 0; nt < 3; ++nt)
+            for (int mt = 0; mt < 2; ++mt) {
+                d[mt][nt][0] += c0;
+                d[mt][nt][1] += c1;
+                d[mt][nt][2] += c0;
+                d[mt][nt][3] += c1;
+                if constexpr (MODE == PLANE_LAYER) {
 #pragma unroll
-                for (int i = 0; i < 4; ++i) e[qq][nt][i] = 0.f;
-#pragma unroll
-        for (int kk = 0; kk < 2; ++kk) {
-            uint32_t A[2][4];
-#pragma unroll
-            for (int qq = 0; qq < 2; ++qq) {
-                A[qq][0] = trans8(P[kk][2 * qq][0]);
-                A[qq][1] = trans8(P[kk][2 * qq + 1][0]);
-                A[qq][2] = trans8(P[kk][2 * qq][1]);
-                A[qq][3] = trans8(P[kk][2 * qq + 1][1]);
-            }
-            const int zz = z0 + 16 * kk + 2 * t4;
-#pragma unroll
-            for (int nt = 0; nt < 3; ++nt) {
-                const int j = nt * 8 + g;
-                const uint32_t b0 = w32(a.tzt, j * 64 + zz), b1 = w32(a.tzt, j * 64 + zz + 8);
-#pragma unroll
-                for (int qq = 0; qq < 2; ++qq) mma(e[qq][nt], A[qq], b0, b1);
+                    for (int q = 0; q < 4; ++q) d[mt][nt][q] = gelu(d[mt][nt][q]);
+                }
             }
         }
-        // e[qq][nt]: channel 16 qq + g (+8 in e[2], e[3]), (re, im) of kz = 4 nt + t4
-        if (half == 1) {
+
+        const int64_t gsite = plane0 + int64_t(y0 + r) * FN + z0;   // global site of the warp's first z
+        if constexpr (MODE == PLANE_LAST) {
+            // out = prior + s_b (Wq2 GELU(Wq1 h + bq1) + bq2), chained through the fragments
+            float nsum = 0.f;
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                uint32_t A1[2][4];
+#pragma unroll
+                for (int ks = 0; ks < 2; ++ks) {
+                    A1[ks][0] = pk(d[mt][2 * ks][0], d[mt][2 * ks][1]);
+                    A1[ks][1] = pk(d[mt][2 * ks][2], d[mt][2 * ks][3]);
+                    A1[ks][2] = pk(d[mt][2 * ks + 1][0], d[mt][2 * ks + 1][1]);
+                    A1[ks][3] = pk(d[mt][2 * ks + 1][2], d[mt][2 * ks + 1][3]);
+                }
+                float q[8][4];
+#pragma unroll
+                for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) q[nt][i] = 0.f;
+#pragma unroll
+                    for (int ks = 0; ks < 2; ++ks) {
+                        const uint2 w = wfrag(a.Wq1, 32, nt * 8 + g, ks, t4);
+                        mma(q[nt], A1[ks], w.x, w.y);
+                    }
+                    const float c0 = a.bq1[nt * 8 + 2 * t4], c1 = a.bq1[nt * 8 + 2 * t4 + 1];
+                    q[nt][0] = gelu(q[nt][0] + c0);
+                    q[nt][1] = gelu(q[nt][1] + c1);
+                    q[nt][2] = gelu(q[nt][2] + c0);
+                    q[nt][3] = gelu(q[nt][3] + c1);
+                }
+                float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int ks = 0; ks < 4; ++ks) {
+                    const uint32_t A2[4] = {pk(q[2 * ks][0], q[2 * ks][1]), pk(q[2 * ks][2], q[2 * ks][3]),
+                                            pk(q[2 * ks + 1][0], q[2 * ks + 1][1]),
+                                            pk(q[2 * ks + 1][2], q[2 * ks + 1][3])};
+                    const uint2 w = wfrag(a.Wq2, 64, g, ks, t4);
+                    mma(o, A2, w.x, w.y);
+                }
+                if (t4 == 0) {
+                    const int64_t s0 = int64_t(b) * FN3 + gsite + 16 * mt + g;
+                    const float2 p0 = a.prior[s0], p1 = a.prior[s0 + 8];
+                    const float2 v0 = make_float2(fmaf(s_b, o[0] + a.bq2[0], p0.x), fmaf(s_b, o[1] + a.bq2[1], p0.y));
+                    const float2 v1 = make_float2(fmaf(s_b, o[2] + a.bq2[0], p1.x), fmaf(s_b, o[3] + a.bq2[1], p1.y));
+                    a.out[s0] = v0;
+                    a.out[s0 + 8] = v1;
+                    nsum += v0.x * v0.x + v0.y * v0.y + v1.x * v1.x + v1.y * v1.y;
+                }
+            }
+            if (a.out_norm) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) nsum += __shfl_xor_sync(0xffffffffu, nsum, o);
+                if (lane == 0) atomicAdd(a.out_norm + b, double(nsum));
+            }
+            __syncthreads();   // every warp is done with this group's h buffer
+            stage(grp + 2);
+            continue;
+        } else {
+            // store h (BF16 channel pairs) and keep the packed fragments for the z-DFT
+            uint32_t P[2][4][2];
+            uint32_t* hb = a.h_out + int64_t(b) * (FC / 2) * FN3;
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                const int64_t s0 = gsite + 16 * mt + g;
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    P[mt][nt][0] = pk(d[mt][nt][0], d[mt][nt][1]);
+                    P[mt][nt][1] = pk(d[mt][nt][2], d[mt][nt][3]);
+                    uint32_t* hp = hb + int64_t(nt * 4 + t4) * FN3;
+                    hp[s0] = P[mt][nt][0];
+                    hp[s0 + 8] = P[mt][nt][1];
+                }
+            }
+            // forward z-DFT over the warp's 32 sites: Y[c][j] = sum_z h[z][c] T[z][j]; the A
+            // operand (channels x sites) is the transpose of the fragments above
+            float e[2][3][4];
 #pragma unroll
             for (int qq = 0; qq < 2; ++qq)
 #pragma unroll
-                for (int nt = 0; nt < 3; ++nt) {
-                    red[r][16 * qq + g][4 * nt + t4] = make_float2(e[qq][nt][0], e[qq][nt][1]);
-                    red[r][16 * qq + g + 8][4 * nt + t4] = make_float2(e[qq][nt][2], e[qq][nt][3]);
+                for (int nt = 0; nt < 3; ++nt)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) e[qq][nt][i] = 0.f;
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+                uint32_t A[2][4];
+#pragma unroll
+                for (int qq = 0; qq < 2; ++qq) {
+                    A[qq][0] = trans8(P[kk][2 * qq][0]);
+                    A[qq][1] = trans8(P[kk][2 * qq + 1][0]);
+                    A[qq][2] = trans8(P[kk][2 * qq][1]);
+                    A[qq][3] = trans8(P[kk][2 * qq + 1][1]);
                 }
-        }
-        __syncthreads();
-        if (half == 0) {
-#pragma unroll
-            for (int qq = 0; qq < 2; ++qq)
 #pragma unroll
                 for (int nt = 0; nt < 3; ++nt) {
-                    const int kz = 4 * nt + t4, c0 = 16 * qq + g;
-                    const float2 u = red[r][c0][kz], v = red[r][c0 + 8][kz];
-                    szbuf[c0][r * FM + kz] = pk(e[qq][nt][0] + u.x, e[qq][nt][1] + u.y);
-                    szbuf[c0 + 8][r * FM + kz] = pk(e[qq][nt][2] + v.x, e[qq][nt][3] + v.y);
+                    const uint2 bz = a.tzt_b[((half * 2 + kk) * 3 + nt) * 32 + lane];
+#pragma unroll
+                    for (int qq = 0; qq < 2; ++qq) mma(e[qq][nt], A[qq], bz.x, bz.y);
                 }
-        }
-        __syncthreads();
-        // the four rows of a channel are contiguous in SZ
-        uint32_t* dst = a.sz + ((int64_t(b) * FC * FN + xcol) * FN + 4 * yg) * FM;
-        for (int i = threadIdx.x; i < FC * 4 * FM; i += 256) {
-            const int c = i / (4 * FM), k = i % (4 * FM);
-            dst[int64_t(c) * FN * FN * FM + k] = szbuf[c][k];
+            }
+            // e[qq][nt]: channel 16 qq + g (+8 in e[2], e[3]), (re, im) of kz = 4 nt + t4
+            if (half == 1) {
+#pragma unroll
+                for (int qq = 0; qq < 2; ++qq)
+#pragma unroll
+                    for (int nt = 0; nt < 3; ++nt) {
+                        sm.red[r][16 * qq + g][4 * nt + t4] = make_float2(e[qq][nt][0], e[qq][nt][1]);
+                        sm.red[r][16 * qq + g + 8][4 * nt + t4] = make_float2(e[qq][nt][2], e[qq][nt][3]);
+                    }
+            }
+            __syncthreads();   // red ready; every warp is done with this group's h buffer
+            stage(grp + 2);
+            if (half == 0) {
+#pragma unroll
+                for (int qq = 0; qq < 2; ++qq)
+#pragma unroll
+                    for (int nt = 0; nt < 3; ++nt) {
+                        const int kz = 4 * nt + t4, c0 = 16 * qq + g;
+                        const float2 u = sm.red[r][c0][kz], v = sm.red[r][c0 + 8][kz];
+                        sm.ys[r * ZS_Y + kz * ZS_KZ + c0] = pk(e[qq][nt][0] + u.x, e[qq][nt][1] + u.y);
+                        sm.ys[r * ZS_Y + kz * ZS_KZ + c0 + 8] = pk(e[qq][nt][2] + v.x, e[qq][nt][3] + v.y);
+                    }
+            }
+            __syncthreads();   // ys ready
+            // 3. forward y DFT over the group's rows: acc[ky'][n] += sum_y F[y][ky'] Y[y][n]
+            //    (interleaved rows: re of ky' = 8 mt + g in rows 0-7, im in rows 8-15)
+#pragma unroll
+            for (int mt = 0; mt < 3; ++mt) {
+                const uint4 f = a.fwd_a[(grp * 3 + mt) * 32 + lane];
+                const uint32_t A[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const int nt = 3 * warp + j, kz = nt >> 2, c = (nt & 3) * 8 + g;
+                    mma(acc[mt][j], A, sm.ys[t4 * ZS_Y + kz * ZS_KZ + c], sm.ys[(t4 + 4) * ZS_Y + kz * ZS_KZ + c]);
+                }
+            }
         }
     }
-}
 
-// y DFT 64 -> 24 kept ky, per (b, c, 8 x-columns); warp w owns column x0 + w:
-// out^T[kz][j] = sum_k A[kz][k] F[k][j], k = 2 y + s (the complex value in(y, kz)).
-__global__ void __launch_bounds__(256) fno_ydft_fwd_kernel(const uint32_t* __restrict__ sz, uint32_t* __restrict__ sy,
-                                                           const uint16_t* __restrict__ fwd, int B) {
-    __shared__ uint32_t slab[8][ZSLAB];
-    __shared__ uint32_t fs[48 * FWD_LD];
-    __shared__ uint32_t obuf[NPK * 8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, t4 = lane & 3;
-    const int xg = blockIdx.x % 8, c = (blockIdx.x / 8) % FC, b = blockIdx.x / (8 * FC);
-    const int x0 = 8 * xg;
-    const uint4* src = reinterpret_cast<const uint4*>(sz + ((int64_t(b) * FC + c) * FN + x0) * ZSLAB);
-    uint4* sl = reinterpret_cast<uint4*>(&slab[0][0]);
-    for (int i = threadIdx.x; i < 8 * ZSLAB / 4; i += 256) sl[i] = src[i];
-    const uint32_t* f32 = reinterpret_cast<const uint32_t*>(fwd);
-    for (int i = threadIdx.x; i < 48 * 64; i += 256) fs[(i / 64) * FWD_LD + i % 64] = f32[i];
-    __syncthreads();
-    float d[6][4];
+    if constexpr (MODE != PLANE_LAST) {
+        // the plane's new y-spectra: (re, im) of ky' = 8 mt + g at n and n+1
 #pragma unroll
-    for (int nt = 0; nt < 6; ++nt)
+        for (int mt = 0; mt < 3; ++mt)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
-    const uint32_t* s = slab[warp];
-    const bool lo = g < FM, hi = g + 8 < FM;
-#pragma unroll
-    for (int ks = 0; ks < 8; ++ks) {
-        const int yy = 8 * ks + t4;
-        const uint32_t A[4] = {lo ? s[yy * FM + g] : 0u, hi ? s[yy * FM + g + 8] : 0u,
-                               lo ? s[(yy + 4) * FM + g] : 0u, hi ? s[(yy + 4) * FM + g + 8] : 0u};
-#pragma unroll
-        for (int nt = 0; nt < 6; ++nt) {
-            const uint32_t* fr = fs + (nt * 8 + g) * FWD_LD + 8 * ks + t4;
-            mma(d[nt], A, fr[0], fr[4]);
-        }
+            for (int j = 0; j < 3; ++j) {
+                const int nt = 3 * warp + j, kz = nt >> 2, c = (nt & 3) * 8 + 2 * t4;
+                const int ky = 8 * mt + g;
+                uint2 v = make_uint2(pk(acc[mt][j][0], acc[mt][j][2]), pk(acc[mt][j][1], acc[mt][j][3]));
+                *reinterpret_cast<uint2*>(syg + (ky * FM + kz) * FC + c) = v;
+            }
     }
-#pragma unroll
-    for (int nt = 0; nt < 6; ++nt) {
-        const int ky = 4 * nt + t4;
-        if (lo) obuf[(ky * FM + g) * 8 + warp] = pk(d[nt][0], d[nt][1]);
-        if (hi) obuf[(ky * FM + g + 8) * 8 + warp] = pk(d[nt][2], d[nt][3]);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < NPK * 8; i += 256) {
-        const int p = i / 8, xi = i % 8;
-        sy[((int64_t(p) * B + b) * FC + c) * FN + x0 + xi] = obuf[i];
-    }
-}
-
-// y DFT 24 kept ky -> 64, per (b, c, 8 x-columns): out^T[kz][j] = sum_k A[kz][k] G[k][j],
-// k = 2 ky' + s, j = 2 y + s'.
-__global__ void __launch_bounds__(256) fno_ydft_inv_kernel(const uint32_t* __restrict__ sy, uint32_t* __restrict__ sz,
-                                                           const uint16_t* __restrict__ inv, int B) {
-    constexpr int IN_LD = NPK + 4;
-    __shared__ uint32_t in[8 * IN_LD];
-    __shared__ uint32_t gs[128 * INV_LD];
-    __shared__ uint32_t obuf[8][ZSLAB];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, t4 = lane & 3;
-    const int xg = blockIdx.x % 8, c = (blockIdx.x / 8) % FC, b = blockIdx.x / (8 * FC);
-    const int x0 = 8 * xg;
-    for (int i = threadIdx.x; i < NPK * 8; i += 256) {
-        const int p = i / 8, xi = i % 8;
-        in[xi * IN_LD + p] = sy[((int64_t(p) * B + b) * FC + c) * FN + x0 + xi];
-    }
-    const uint32_t* g32 = reinterpret_cast<const uint32_t*>(inv);
-    for (int i = threadIdx.x; i < 128 * 24; i += 256) gs[(i / 24) * INV_LD + i % 24] = g32[i];
-    __syncthreads();
-    float d[16][4];
-#pragma unroll
-    for (int nt = 0; nt < 16; ++nt)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
-    const uint32_t* s = in + warp * IN_LD;
-    const bool lo = g < FM, hi = g + 8 < FM;
-#pragma unroll
-    for (int ks = 0; ks < 3; ++ks) {
-        const int ky = 8 * ks + t4;
-        const uint32_t A[4] = {lo ? s[ky * FM + g] : 0u, hi ? s[ky * FM + g + 8] : 0u,
-                               lo ? s[(ky + 4) * FM + g] : 0u, hi ? s[(ky + 4) * FM + g + 8] : 0u};
-#pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            const uint32_t* gr = gs + (nt * 8 + g) * INV_LD + 8 * ks + t4;
-            mma(d[nt], A, gr[0], gr[4]);
-        }
-    }
-#pragma unroll
-    for (int nt = 0; nt < 16; ++nt) {
-        const int yy = 4 * nt + t4;
-        if (lo) obuf[warp][yy * FM + g] = pk(d[nt][0], d[nt][1]);
-        if (hi) obuf[warp][yy * FM + g + 8] = pk(d[nt][2], d[nt][3]);
-    }
-    __syncthreads();
-    uint4* dst = reinterpret_cast<uint4*>(sz + ((int64_t(b) * FC + c) * FN + x0) * ZSLAB);
-    const uint4* ob = reinterpret_cast<const uint4*>(&obuf[0][0]);
-    for (int i = threadIdx.x; i < 8 * ZSLAB / 4; i += 256) dst[i] = ob[i];
 }
 
 // x DFT of one kept (ky, kz) for 16 samples, the channel mixing of its 24 modes, and
-// the inverse x DFT, in place on SY. Rows are (sample, channel), 64 x values each.
+// the inverse x DFT, in place on SY. Rows are (sample, channel), 64 x values each; a
+// row's values lie SYW words apart (SY is [b][x][(ky', kz)][c]).
 struct XmixSmem {
     uint32_t fs[48 * FWD_LD];
     uint32_t gs[128 * INV_LD];
@@ -506,7 +625,8 @@ __global__ void __launch_bounds__(256) fno_xmix_kernel(uint32_t* __restrict__ sy
     const int g = lane >> 2, t4 = lane & 3;
     const int p = blockIdx.x % NPK, b0 = 16 * (blockIdx.x / NPK);
     const int nb = B - b0 < 16 ? B - b0 : 16;
-    uint32_t* base = sy + (int64_t(p) * B + b0) * FC * FN;   // row (sample, channel), x
+    uint32_t* base = sy + p * FC;
+    auto at = [&](int row, int xx) { return (int64_t(b0 + row / FC) * FN + xx) * SYW + row % FC; };
     const uint32_t* f32 = reinterpret_cast<const uint32_t*>(fwd);
     for (int i = threadIdx.x; i < 48 * 64; i += 256) sm.fs[(i / 64) * FWD_LD + i % 64] = f32[i];
     const uint32_t* g32 = reinterpret_cast<const uint32_t*>(inv);
@@ -526,8 +646,8 @@ __global__ void __launch_bounds__(256) fno_xmix_kernel(uint32_t* __restrict__ sy
 #pragma unroll
         for (int ks = 0; ks < 8; ++ks) {
             const int xx = 8 * ks + t4;
-            const uint32_t A[4] = {v0 ? base[r0 * FN + xx] : 0u, v1 ? base[r1 * FN + xx] : 0u,
-                                   v0 ? base[r0 * FN + xx + 4] : 0u, v1 ? base[r1 * FN + xx + 4] : 0u};
+            const uint32_t A[4] = {v0 ? base[at(r0, xx)] : 0u, v1 ? base[at(r1, xx)] : 0u,
+                                   v0 ? base[at(r0, xx + 4)] : 0u, v1 ? base[at(r1, xx + 4)] : 0u};
 #pragma unroll
             for (int nt = 0; nt < 6; ++nt) {
                 const uint32_t* fr = sm.fs + (nt * 8 + g) * FWD_LD + 8 * ks + t4;
@@ -561,9 +681,10 @@ __global__ void __launch_bounds__(256) fno_xmix_kernel(uint32_t* __restrict__ sy
         for (int nt = 0; nt < 8; ++nt) {
             float z[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-            for (int ks = 0; ks < 4; ++ks)
-                mma(z, A[ks], w32(wm, (nt * 8 + g) * 64 + 16 * ks + 2 * t4),
-                    w32(wm, (nt * 8 + g) * 64 + 16 * ks + 8 + 2 * t4));
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint2 w = wfrag(wm, 64, nt * 8 + g, ks, t4);
+                mma(z, A[ks], w.x, w.y);
+            }
             const int o = 4 * nt + t4;
             hk[g * HS_B + o] = pk(z[0], z[1]);
             hk[(g + 8) * HS_B + o] = pk(z[2], z[3]);
@@ -596,21 +717,22 @@ __global__ void __launch_bounds__(256) fno_xmix_kernel(uint32_t* __restrict__ sy
 #pragma unroll
         for (int nt = 0; nt < 16; ++nt) {
             const int xx = 4 * nt + t4;
-            if (v0) base[r0 * FN + xx] = pk(d[nt][0], d[nt][1]);
-            if (v1) base[r1 * FN + xx] = pk(d[nt][2], d[nt][3]);
+            if (v0) base[at(r0, xx)] = pk(d[nt][0], d[nt][1]);
+            if (v1) base[at(r1, xx)] = pk(d[nt][2], d[nt][3]);
         }
     }
 }
 
-// Wi[mode][n][k] = M'[k][n] with k = 2 i + s, n = 2 o + s' (interleaved real/imaginary):
-// M'[2i][2o] = Rr, M'[2i+1][2o] = -Ri, M'[2i][2o+1] = Ri, M'[2i+1][2o+1] = Rr.
+// Wi[mode][n][d] = M'[k][n], k = frag_src_col(d), with k = 2 i + s, n = 2 o + s'
+// (interleaved real/imaginary): M'[2i][2o] = Rr, M'[2i+1][2o] = -Ri, M'[2i][2o+1] = Ri,
+// M'[2i+1][2o+1] = Rr.
 __global__ void pack_mix_interleaved_kernel(const float* __restrict__ R, __nv_bfloat16* __restrict__ Wi, int C,
                                             int nmodes) {
     const int K2 = 2 * C;
     const int64_t total = int64_t(nmodes) * K2 * K2;
     for (int64_t gi = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; gi < total;
          gi += int64_t(gridDim.x) * blockDim.x) {
-        const int k = int(gi % K2), n = int((gi / K2) % K2);
+        const int k = frag_src_col(int(gi % K2)), n = int((gi / K2) % K2);
         const int64_t mode = gi / (int64_t(K2) * K2);
         const int i = k >> 1, s = k & 1, o = n >> 1, so = n & 1;
         const float* rr = R + ((mode * C + i) * C + o) * 2;
@@ -619,12 +741,13 @@ __global__ void pack_mix_interleaved_kernel(const float* __restrict__ R, __nv_bf
     }
 }
 
-// dst[r][c] = src[r][c] as bf16 for r < rows, c < cols, zero elsewhere (rows_pad x cols_pad)
+// dst[r][c] = src[r][c'] as bf16 for r < rows, c' < cols, zero elsewhere (rows_pad x
+// cols_pad); c' = c, or frag_src_col(c) in fragment order
 __global__ void to_bf16_kernel(const float* __restrict__ src, int rows, int cols, __nv_bfloat16* __restrict__ dst,
-                               int rows_pad, int cols_pad) {
+                               int rows_pad, int cols_pad, int frag) {
     const int n = rows_pad * cols_pad;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int r = i / cols_pad, c = i % cols_pad;
+        const int r = i / cols_pad, c = frag ? frag_src_col(i % cols_pad) : i % cols_pad;
         dst[i] = __float2bfloat16_rn(r < rows && c < cols ? src[r * cols + c] : 0.f);
     }
 }
@@ -633,15 +756,28 @@ int st(cudaError_t e) { return e == cudaSuccess ? WFS_OK : WFS_ERR_CUDA; }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
-int launch_zrow(int mode, ZrowArgs& a, cudaStream_t s) {
+template <int MODE>
+int launch_plane(PlaneArgs& a, int B, cudaStream_t s) {
     const FastTables* t = fast_tables();
     if (!t) return WFS_ERR_CUDA;
-    a.tz = t->tz;
-    a.tzt = t->tzt;
-    const unsigned grid = unsigned(a.B) * FN * 16;
-    if (mode == ZROW_LIFT) fno_zrow_kernel<ZROW_LIFT><<<grid, 256, 0, s>>>(a);
-    else if (mode == ZROW_LAYER) fno_zrow_kernel<ZROW_LAYER><<<grid, 256, 0, s>>>(a);
-    else fno_zrow_kernel<ZROW_LAST><<<grid, 256, 0, s>>>(a);
+    a.inv_a = t->inv_a;
+    a.fwd_a = t->fwd_a;
+    a.tz_a = t->tz_a;
+    a.tzt_b = t->tzt_b;
+    static std::mutex mu;
+    static std::map<int, bool> attr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return WFS_ERR_CUDA;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!attr[dev]) {
+            if (cudaFuncSetAttribute(fno_plane_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(sizeof(PlaneSmem))) != cudaSuccess)
+                return WFS_ERR_CUDA;
+            attr[dev] = true;
+        }
+    }
+    fno_plane_kernel<MODE><<<unsigned(B) * FN, PT, sizeof(PlaneSmem), s>>>(a);
     return st(cudaGetLastError());
 }
 
@@ -652,41 +788,51 @@ using namespace wfs;
 
 extern "C" {
 
-int wfs_fno_fast_lift(const void* x, const void* W0p, const float* b0, void* h, void* sz, int32_t B, void* stream) {
-    if (!x || !W0p || !b0 || !h || !sz || B < 1 || !aligned16(sz)) return WFS_ERR_ARG;
-    ZrowArgs a;
+int wfs_fno_fast_lift(const void* psi, int64_t psi_stride, const void* V, int64_t v_stride, float vscale,
+                      const double* a2, const void* W0p, const float* b0, void* h, void* sy, int32_t B,
+                      void* stream) {
+    if (!psi || !V || !W0p || !b0 || !h || !sy || B < 1 || !aligned16(psi) || !aligned16(V) || !aligned16(h) ||
+        !aligned16(sy) || (psi_stride & 1) || (v_stride & 1))
+        return WFS_ERR_ARG;
+    PlaneArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.x = static_cast<const float2*>(x);
+    a.psi = static_cast<const float2*>(psi);
+    a.V = static_cast<const float2*>(V);
+    a.psi_stride = psi_stride;
+    a.v_stride = v_stride;
+    a.vscale = vscale;
+    a.a2 = a2;
     a.W = static_cast<const uint16_t*>(W0p);
     a.bias = b0;
     a.h_out = static_cast<uint32_t*>(h);
-    a.sz = static_cast<uint32_t*>(sz);
-    a.B = B;
-    return launch_zrow(ZROW_LIFT, a, static_cast<cudaStream_t>(stream));
+    a.sy = static_cast<uint32_t*>(sy);
+    return launch_plane<PLANE_LIFT>(a, B, static_cast<cudaStream_t>(stream));
 }
 
-int wfs_fno_fast_layer(const void* h_in, void* sz, const void* W, const float* bias, void* h_out, int32_t B,
+int wfs_fno_fast_layer(const void* h_in, void* sy, const void* W, const float* bias, void* h_out, int32_t B,
                        void* stream) {
-    if (!h_in || !sz || !W || !bias || !h_out || h_in == h_out || B < 1 || !aligned16(sz)) return WFS_ERR_ARG;
-    ZrowArgs a;
+    if (!h_in || !sy || !W || !bias || !h_out || h_in == h_out || B < 1 || !aligned16(h_in) || !aligned16(sy))
+        return WFS_ERR_ARG;
+    PlaneArgs a;
     std::memset(&a, 0, sizeof(a));
     a.h = static_cast<const uint32_t*>(h_in);
-    a.sz = static_cast<uint32_t*>(sz);
+    a.sy = static_cast<uint32_t*>(sy);
     a.W = static_cast<const uint16_t*>(W);
     a.bias = bias;
     a.h_out = static_cast<uint32_t*>(h_out);
-    a.B = B;
-    return launch_zrow(ZROW_LAYER, a, static_cast<cudaStream_t>(stream));
+    return launch_plane<PLANE_LAYER>(a, B, static_cast<cudaStream_t>(stream));
 }
 
-int wfs_fno_fast_last(const void* h_in, const void* sz, const void* W, const float* bias, const void* Wq1,
-                      const float* bq1, const void* Wq2p, const float* bq2, const void* prior, void* out, int32_t B,
-                      void* stream) {
-    if (!h_in || !sz || !W || !bias || !Wq1 || !bq1 || !Wq2p || !bq2 || !prior || !out || B < 1) return WFS_ERR_ARG;
-    ZrowArgs a;
+int wfs_fno_fast_last(const void* h_in, const void* sy, const void* W, const float* bias, const void* Wq1,
+                      const float* bq1, const void* Wq2p, const float* bq2, const void* prior, const double* a2,
+                      void* out, double* out_norm, int32_t B, void* stream) {
+    if (!h_in || !sy || !W || !bias || !Wq1 || !bq1 || !Wq2p || !bq2 || !prior || !out || B < 1 ||
+        !aligned16(h_in) || !aligned16(sy))
+        return WFS_ERR_ARG;
+    PlaneArgs a;
     std::memset(&a, 0, sizeof(a));
     a.h = static_cast<const uint32_t*>(h_in);
-    a.sz = const_cast<uint32_t*>(static_cast<const uint32_t*>(sz));
+    a.sy = const_cast<uint32_t*>(static_cast<const uint32_t*>(sy));
     a.W = static_cast<const uint16_t*>(W);
     a.bias = bias;
     a.Wq1 = static_cast<const uint16_t*>(Wq1);
@@ -694,25 +840,10 @@ int wfs_fno_fast_last(const void* h_in, const void* sz, const void* W, const flo
     a.Wq2 = static_cast<const uint16_t*>(Wq2p);
     a.bq2 = bq2;
     a.prior = static_cast<const float2*>(prior);
+    a.a2 = a2;
     a.out = static_cast<float2*>(out);
-    a.B = B;
-    return launch_zrow(ZROW_LAST, a, static_cast<cudaStream_t>(stream));
-}
-
-int wfs_fno_fast_ydft(const void* src, void* dst, int32_t dir, int32_t B, void* stream) {
-    if (!src || !dst || src == dst || B < 1 || (dir != -1 && dir != 1) || !aligned16(src) || !aligned16(dst))
-        return WFS_ERR_ARG;
-    const FastTables* t = fast_tables();
-    if (!t) return WFS_ERR_CUDA;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const unsigned grid = unsigned(B) * FC * 8;
-    if (dir < 0)
-        fno_ydft_fwd_kernel<<<grid, 256, 0, s>>>(static_cast<const uint32_t*>(src), static_cast<uint32_t*>(dst),
-                                                 t->fwd, B);
-    else
-        fno_ydft_inv_kernel<<<grid, 256, 0, s>>>(static_cast<const uint32_t*>(src), static_cast<uint32_t*>(dst),
-                                                 t->inv, B);
-    return st(cudaGetLastError());
+    a.out_norm = out_norm;
+    return launch_plane<PLANE_LAST>(a, B, static_cast<cudaStream_t>(stream));
 }
 
 int wfs_fno_fast_xmix(void* sy, const void* Wi, int32_t B, void* stream) {
@@ -748,11 +879,12 @@ int wfs_fno_pack_mix_interleaved(const float* R, void* Wi, int32_t C, int32_t nm
 }
 
 int wfs_fno_to_bf16(const float* src, int32_t rows, int32_t cols, void* dst, int32_t rows_pad, int32_t cols_pad,
-                    void* stream) {
-    if (!src || !dst || rows < 1 || cols < 1 || rows_pad < rows || cols_pad < cols) return WFS_ERR_ARG;
+                    int32_t frag_order, void* stream) {
+    if (!src || !dst || rows < 1 || cols < 1 || rows_pad < rows || cols_pad < cols || (frag_order && (cols_pad & 15)))
+        return WFS_ERR_ARG;
     const int n = rows_pad * cols_pad;
     to_bf16_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        src, rows, cols, static_cast<__nv_bfloat16*>(dst), rows_pad, cols_pad);
+        src, rows, cols, static_cast<__nv_bfloat16*>(dst), rows_pad, cols_pad, frag_order ? 1 : 0);
     return st(cudaGetLastError());
 }
 

@@ -176,7 +176,7 @@ class FNO:
             for name, dst in self.fast_w.items():
                 rows, cols = self.offsets[name][1]
                 self._ck(self.lib.wfs_fno_to_bf16(_ptr(self.view(name)), rows, cols, _ptr(dst), dst.shape[0],
-                                                  dst.shape[1], self._s()), "to_bf16")
+                                                  dst.shape[1], 1, self._s()), "to_bf16")
             for l in range(self.cfg.layers):
                 self._ck(self.lib.wfs_fno_pack_mix_interleaved(_ptr(self.view(f"R{l + 1}")), _ptr(self.fast_mix[l]),
                                                                c, self.cfg.nmodes, self._s()), "pack_mix")
@@ -251,38 +251,49 @@ class FNO:
         i32 = dict(dtype=torch.int32, device=self.device)
         self.fast_ws = None
         self.fast_ws = {"h": [torch.empty((B, cfg.width // 2, cfg.n3), **i32) for _ in range(2)],
-                        "sz": torch.empty((B, cfg.width, cfg.N, cfg.N, cfg.modes), **i32),
-                        "sy": torch.empty((2 * cfg.modes, cfg.modes, B, cfg.width, cfg.N), **i32),
+                        "sy": torch.empty((B, cfg.N, 2 * cfg.modes, cfg.modes, cfg.width), **i32),
                         "out": torch.empty((B, cfg.n3), dtype=torch.complex64, device=self.device)}
         self.fast_batch = B
         return self.fast_ws
 
     def forward_fast(self, x, prior, B, out=None):
         """The same network as forward() for inference, on the kept modes only (csrc/fno_fast.cu):
-        BF16 tensor-core products with FP32 accumulation and BF16 intermediates, the z-DFTs fused
-        into the pointwise layers. Geometry N = 64, width 32, 12 modes, projection width 64."""
+        BF16 tensor-core products with FP32 accumulation and BF16 intermediates, one plane
+        kernel per layer. x: [B][2][n3] normalised input, prior: [B][n3] normalised prior.
+        Geometry N = 64, width 32, 12 modes, projection width 64."""
+        n3 = self.cfg.n3
+        return self._fast(x, 2 * n3, x[:, 1], 2 * n3, 1.0, None, prior, B, out, None)
+
+    def jump_fast(self, psi, V, prior, a2, B, out=None, out_norm=None):
+        """One surrogate jump on raw fields: out = prior + s_b FNO(psi / s_b, V vscale), with
+        s_b = sqrt(a2_b / n3) (a2 from wfs_fno_sample_norms of psi). psi, V, prior:
+        [B][n3] complex64; out_norm (optional, B doubles, zeroed by the caller) receives
+        sum |out_b|^2."""
+        n3 = self.cfg.n3
+        return self._fast(psi, n3, V, n3, float(self.cfg.vscale), a2, prior, B, out, out_norm)
+
+    def _fast(self, f0, s0, f1, s1, vscale, a2, prior, B, out, out_norm):
         if not self.fast_ok:
-            raise ValueError(f"forward_fast supports (N, width, modes, hidden) = {FAST_GEOMETRY}")
+            raise ValueError(f"the inference kernels support (N, width, modes, hidden) = {FAST_GEOMETRY}")
         cfg, lib, s, ck = self.cfg, self.lib, self._s(), self._ck
+        # the kernels address SY and H with the B they are given: a smaller batch uses the
+        # leading part of each buffer
         ws = self.fast_workspace(B)
-        # the kernels address SY, SZ and H with the B they are given: a smaller batch uses
-        # the leading part of each buffer
-        sz, sy, h, L = ws["sz"], ws["sy"], ws["h"], cfg.layers
-        fw = self.fast_w
+        sy, h, L, fw = ws["sy"], ws["h"], cfg.layers, self.fast_w
         dst = ws["out"] if out is None else out
-        ck(lib.wfs_fno_fast_lift(_ptr(x), _ptr(fw["W0"]), _ptr(self.view("b0")), _ptr(h[0]), _ptr(sz), B, s), "lift")
+        ck(lib.wfs_fno_fast_lift(_ptr(f0), s0, _ptr(f1), s1, vscale, _ptr(a2), _ptr(fw["W0"]), _ptr(self.view("b0")),
+                                 _ptr(h[0]), _ptr(sy), B, s), "lift")
         for l in range(L):
-            ck(lib.wfs_fno_fast_ydft(_ptr(sz), _ptr(sy), -1, B, s), "ydft")
             ck(lib.wfs_fno_fast_xmix(_ptr(sy), _ptr(self.fast_mix[l]), B, s), "xmix")
-            ck(lib.wfs_fno_fast_ydft(_ptr(sy), _ptr(sz), 1, B, s), "ydft inverse")
             hin, hout = h[l % 2], h[(l + 1) % 2]
             if l < L - 1:
-                ck(lib.wfs_fno_fast_layer(_ptr(hin), _ptr(sz), _ptr(fw[f"W{l + 1}"]), _ptr(self.view(f"b{l + 1}")),
+                ck(lib.wfs_fno_fast_layer(_ptr(hin), _ptr(sy), _ptr(fw[f"W{l + 1}"]), _ptr(self.view(f"b{l + 1}")),
                                           _ptr(hout), B, s), "layer")
             else:
-                ck(lib.wfs_fno_fast_last(_ptr(hin), _ptr(sz), _ptr(fw[f"W{l + 1}"]), _ptr(self.view(f"b{l + 1}")),
+                ck(lib.wfs_fno_fast_last(_ptr(hin), _ptr(sy), _ptr(fw[f"W{l + 1}"]), _ptr(self.view(f"b{l + 1}")),
                                          _ptr(fw["Wq1"]), _ptr(self.view("bq1")), _ptr(fw["Wq2"]),
-                                         _ptr(self.view("bq2")), _ptr(prior), _ptr(dst), B, s), "last")
+                                         _ptr(self.view("bq2")), _ptr(prior), _ptr(a2), _ptr(dst), _ptr(out_norm), B,
+                                         s), "last")
         return dst[:B]
 
     def _wgrad(self, g, cout, x, cin, name_w, B):
