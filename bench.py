@@ -595,16 +595,18 @@ def surrogate_distribution(args, dist, stream):
     lib = model.lib
     sp = ctypes.c_void_p(stream.cuda_stream)
     out = torch.empty_like(prior)
+    out_norm = torch.zeros(G, dtype=torch.float64, device=stream.device)
 
     def infer():
+        # |psi|^2 per sample (normalisation), then the jump on raw fields: the lift divides by
+        # the RMS, the last layer adds s_b * network to the raw prior and accumulates |out|^2
+        # for the norm test
         lib.wfs_fno_sample_norms(F._ptr(psi), None, cfg.n3, G, F._ptr(a2), None, sp)
-        lib.wfs_fno_make_input(F._ptr(psi), F._ptr(gen.V), float(cfg.vscale), F._ptr(a2), F._ptr(x), G, cfg.n3, sp)
-        lib.wfs_fno_scale_samples(F._ptr(prior), F._ptr(a2), 1, G, cfg.n3, sp)
-        model.forward_fast(x, prior, G, out=out)
-        lib.wfs_fno_scale_samples(F._ptr(out), F._ptr(a2), 0, G, cfg.n3, sp)
-        lib.wfs_fno_sample_norms(F._ptr(out), None, cfg.n3, G, F._ptr(a2), None, sp)
+        out_norm.zero_()
+        model.jump_fast(psi, gen.V, prior, a2, G, out=out, out_norm=out_norm)
 
     def infer_f32():
+        lib.wfs_fno_make_input(F._ptr(psi), F._ptr(gen.V), float(cfg.vscale), F._ptr(a2), F._ptr(x), G, cfg.n3, sp)
         for k in range(0, G, 16):
             model.forward(x[k:k + 16], prior[k:k + 16], 16, out=out[k:k + 16], keep_pre=False)
 
@@ -674,7 +676,8 @@ def run_surrogate(args):
             "data": "synthetic",
             "config": {"workload": "FNO 64^3 width 32 modes 12 layers 4, K=50, jump = coarse prior + network",
                        "headline_distribution": dists[0]},
-            "gpu_launches_per_forward": 17,
+            "gpu_launches_per_jump": {"network": 9, "sample_norms": 2,
+                                      "note": "lift, 4 x (mixing, layer), the last layer fused with both projections"},
             "distributions": res}
     if "cpu_seconds_per_jump" in head:
         line["cpu_baseline"] = {"value": 1.0 / head["cpu_seconds_per_jump"], "unit": "jumps/s", "cores": 1,

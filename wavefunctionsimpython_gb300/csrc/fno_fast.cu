@@ -231,18 +231,18 @@ __device__ __forceinline__ uint2 wfrag(const uint16_t* W, int ld, int n, int ks,
 
 // ---------------------------------------------------------------------------
 // Plane kernel: one CTA (16 warps) per (sample b, column x) owns the yz-plane of 64 z-rows
-// and walks it in 8 groups of 8 rows. Per group:
-//   1. inverse y DFT of the layer's spectral branch, from the plane's y-spectra (SY, in
-//      shared memory) to the group's z-spectra (zs)
-//   2. per warp (row r = w/2, sites z in [32 (w&1), +32)): the pointwise product W h and
-//      the inverse z-DFT T . zs accumulate into one set of fragments; bias, GELU, the BF16
-//      store of the new h; the forward z-DFT of the new h over the warp's 32 sites
-//   3. the two half-rows' z-spectra are summed into ys, and the forward y DFT over the
-//      group's 8 rows accumulates into the plane's new y-spectra (registers)
+// and walks it in 8 groups of 8 rows. Per group, between two block barriers:
+//   A. per warp (row r = w/2, sites z in [32 (w&1), +32)): the pointwise product W h and
+//      the inverse z-DFT T . zs of the layer's spectral branch accumulate into one set of
+//      fragments; bias, GELU, the BF16 store of the new h; the forward z-DFT of the new h
+//      over the warp's 32 sites, as FP32 partial sums in red[half]
+//   B. the forward y DFT of this group (the two half-rows' partials summed as they are
+//      read) accumulates into the plane's new y-spectra (registers), and the inverse y DFT
+//      of the next group's rows fills zs from the plane's y-spectra in shared memory
 // The group's h arrives in shared memory by cp.async two groups ahead. After the last
 // group the new y-spectra are stored over SY[b][x] (read whole at the start: in place).
-// The lift reads psi and V instead of h and skips step 1; the last layer stops after the
-// projections of step 2.
+// The lift reads psi and V instead of h and has no spectral branch; the last layer
+// stops after the projections of step A.
 // ---------------------------------------------------------------------------
 constexpr int PT = 512;                 // threads per plane CTA
 constexpr int GROWS = 8;                // z-rows per group
@@ -252,12 +252,13 @@ constexpr int ZS_KZ = FC + 8;           // words per kz of a row's z-spectra
 constexpr int ZS_Y = FM * ZS_KZ + 8;    // words per row of the group's z-spectra
 constexpr int HS_P = GROWS * FN + 8;    // words per channel pair of the staged h
 constexpr int SYW = NPK * FC;           // words of one plane's y-spectra in global memory
+constexpr int RD_KZ = 2 * FC + 8;       // words per kz of a row's FP32 partial z-spectra (float2 per channel)
+constexpr int RD_Y = FM * RD_KZ + 8;    // words per row of the partial z-spectra
 
 struct PlaneSmem {
     uint32_t sy[FK * SY_KS];
     uint32_t zs[GROWS * ZS_Y];
-    uint32_t ys[GROWS * ZS_Y];
-    float2 red[GROWS][FC][FM];
+    float red[2][GROWS * RD_Y];         // [half][row][kz][channel][re, im]
     uint32_t hs[2][(FC / 2) * HS_P];
 };
 
@@ -345,35 +346,39 @@ __global__ void __launch_bounds__(PT, 1) fno_plane_kernel(const PlaneArgs a) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
 
+    // inverse y DFT of group grp: zs[row][kz][c] = sum_ky' G[y][ky'] SY[ky'][kz][c] (interleaved
+    // rows: re of y0+g in rows 0-7, im in rows 8-15); warp w owns n-tiles 3w..3w+2 of (kz, c)
+    auto inverse_y = [&](int grp) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int nt = 3 * warp + j, kz = nt >> 2, c = (nt & 3) * 8 + g;
+            float d[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int ks = 0; ks < 3; ++ks) {
+                const uint4 f = a.inv_a[(grp * 3 + ks) * 32 + lane];
+                const uint32_t A[4] = {f.x, f.y, f.z, f.w};
+                const int ky = 8 * ks + t4;
+                mma(d, A, sm.sy[ky * SY_KS + kz * FC + c], sm.sy[(ky + 4) * SY_KS + kz * FC + c]);
+            }
+            const int cc = (nt & 3) * 8 + 2 * t4;
+            sm.zs[g * ZS_Y + kz * ZS_KZ + cc] = pk(d[0], d[2]);
+            sm.zs[g * ZS_Y + kz * ZS_KZ + cc + 1] = pk(d[1], d[3]);
+        }
+    };
+    if constexpr (MODE != PLANE_LIFT) {
+        cp_wait1();
+        __syncthreads();   // sy and group 0's h have landed
+        inverse_y(0);
+    } else {
+        cp_wait1();
+    }
+
     for (int grp = 0; grp < NGROUP; ++grp) {
         const int y0 = grp * GROWS;
         const uint32_t* hs = sm.hs[grp & 1];
-        if constexpr (MODE != PLANE_LIFT) {
-            cp_wait1();
-            __syncthreads();   // sy (first group) and this group's h have landed
-            // 1. inverse y DFT: zs[row][kz][c] = sum_ky' G[y][ky'] SY[ky'][kz][c] (interleaved rows:
-            //    re of y0+g in rows 0-7, im in rows 8-15)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const int nt = 3 * warp + j, kz = nt >> 2, c = (nt & 3) * 8 + g;
-                float d[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-                for (int ks = 0; ks < 3; ++ks) {
-                    const uint4 f = a.inv_a[(grp * 3 + ks) * 32 + lane];
-                    const uint32_t A[4] = {f.x, f.y, f.z, f.w};
-                    const int ky = 8 * ks + t4;
-                    mma(d, A, sm.sy[ky * SY_KS + kz * FC + c], sm.sy[(ky + 4) * SY_KS + kz * FC + c]);
-                }
-                const int cc = (nt & 3) * 8 + 2 * t4;
-                sm.zs[g * ZS_Y + kz * ZS_KZ + cc] = pk(d[0], d[2]);
-                sm.zs[g * ZS_Y + kz * ZS_KZ + cc + 1] = pk(d[1], d[3]);
-            }
-        } else {
-            cp_wait1();
-        }
-        __syncthreads();   // zs ready (and, for the lift, this group's input)
+        __syncthreads();   // this group's h and zs are ready; red is free
 
-        // 2. pointwise + inverse z-DFT for this warp's 32 sites
+        // A. pointwise + inverse z-DFT for this warp's 32 sites
         const int rowsite = r * FN + z0;   // local site of the warp's first z
         float d[2][4][4];
 #pragma unroll
@@ -509,9 +514,6 @@ __global__ void __launch_bounds__(PT, 1) fno_plane_kernel(const PlaneArgs a) {
                 for (int o = 16; o > 0; o >>= 1) nsum += __shfl_xor_sync(0xffffffffu, nsum, o);
                 if (lane == 0) atomicAdd(a.out_norm + b, double(nsum));
             }
-            __syncthreads();   // every warp is done with this group's h buffer
-            stage(grp + 2);
-            continue;
         } else {
             // store h (BF16 channel pairs) and keep the packed fragments for the z-DFT
             uint32_t P[2][4][2];
@@ -555,42 +557,46 @@ __global__ void __launch_bounds__(PT, 1) fno_plane_kernel(const PlaneArgs a) {
                 }
             }
             // e[qq][nt]: channel 16 qq + g (+8 in e[2], e[3]), (re, im) of kz = 4 nt + t4
-            if (half == 1) {
+            float* rd = sm.red[half] + r * RD_Y;
 #pragma unroll
-                for (int qq = 0; qq < 2; ++qq)
+            for (int qq = 0; qq < 2; ++qq)
 #pragma unroll
-                    for (int nt = 0; nt < 3; ++nt) {
-                        sm.red[r][16 * qq + g][4 * nt + t4] = make_float2(e[qq][nt][0], e[qq][nt][1]);
-                        sm.red[r][16 * qq + g + 8][4 * nt + t4] = make_float2(e[qq][nt][2], e[qq][nt][3]);
-                    }
+                for (int nt = 0; nt < 3; ++nt) {
+                    float* p = rd + (4 * nt + t4) * RD_KZ + 2 * (16 * qq + g);
+                    *reinterpret_cast<float2*>(p) = make_float2(e[qq][nt][0], e[qq][nt][1]);
+                    *reinterpret_cast<float2*>(p + 16) = make_float2(e[qq][nt][2], e[qq][nt][3]);
+                }
+        }
+        __syncthreads();   // red ready; this group's h buffer and zs are free
+        stage(grp + 2);
+        if constexpr (MODE != PLANE_LAST) {
+            // B. forward y DFT over the group's rows: acc[ky'][n] += sum_y F[y][ky'] Y[y][n]
+            //    (interleaved rows: re of ky' = 8 mt + g in rows 0-7, im in rows 8-15), with
+            //    Y the sum of the two half-rows' partials
+            uint32_t Bf[3][2];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int nt = 3 * warp + j, kz = nt >> 2, c = (nt & 3) * 8 + g;
+#pragma unroll
+                for (int h2 = 0; h2 < 2; ++h2) {
+                    const int off = (t4 + 4 * h2) * RD_Y + kz * RD_KZ + 2 * c;
+                    const float2 u = *reinterpret_cast<const float2*>(sm.red[0] + off);
+                    const float2 v = *reinterpret_cast<const float2*>(sm.red[1] + off);
+                    Bf[j][h2] = pk(u.x + v.x, u.y + v.y);
+                }
             }
-            __syncthreads();   // red ready; every warp is done with this group's h buffer
-            stage(grp + 2);
-            if (half == 0) {
-#pragma unroll
-                for (int qq = 0; qq < 2; ++qq)
-#pragma unroll
-                    for (int nt = 0; nt < 3; ++nt) {
-                        const int kz = 4 * nt + t4, c0 = 16 * qq + g;
-                        const float2 u = sm.red[r][c0][kz], v = sm.red[r][c0 + 8][kz];
-                        sm.ys[r * ZS_Y + kz * ZS_KZ + c0] = pk(e[qq][nt][0] + u.x, e[qq][nt][1] + u.y);
-                        sm.ys[r * ZS_Y + kz * ZS_KZ + c0 + 8] = pk(e[qq][nt][2] + v.x, e[qq][nt][3] + v.y);
-                    }
-            }
-            __syncthreads();   // ys ready
-            // 3. forward y DFT over the group's rows: acc[ky'][n] += sum_y F[y][ky'] Y[y][n]
-            //    (interleaved rows: re of ky' = 8 mt + g in rows 0-7, im in rows 8-15)
 #pragma unroll
             for (int mt = 0; mt < 3; ++mt) {
                 const uint4 f = a.fwd_a[(grp * 3 + mt) * 32 + lane];
                 const uint32_t A[4] = {f.x, f.y, f.z, f.w};
 #pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    const int nt = 3 * warp + j, kz = nt >> 2, c = (nt & 3) * 8 + g;
-                    mma(acc[mt][j], A, sm.ys[t4 * ZS_Y + kz * ZS_KZ + c], sm.ys[(t4 + 4) * ZS_Y + kz * ZS_KZ + c]);
-                }
+                for (int j = 0; j < 3; ++j) mma(acc[mt][j], A, Bf[j][0], Bf[j][1]);
             }
         }
+        if constexpr (MODE != PLANE_LIFT) {
+            if (grp + 1 < NGROUP) inverse_y(grp + 1);
+        }
+        cp_wait1();   // the next group's h has landed (visible after the next barrier)
     }
 
     if constexpr (MODE != PLANE_LAST) {
