@@ -37,6 +37,7 @@
 
 #include "../../include/wfs.h"
 #include "../../include/wfs_fno.h"
+#include "bulk_copy.cuh"
 
 namespace wfs {
 namespace {
@@ -47,8 +48,6 @@ constexpr int FM = 12;                 // kept kz
 constexpr int FK = 24;                 // kept kx and ky
 constexpr int64_t FN3 = int64_t(FN) * FN * FN;
 constexpr int NPK = FK * FM;           // kept (ky, kz) pairs
-constexpr int FWD_LD = 68;             // forward DFT matrix row stride in smem (words)
-constexpr int INV_LD = 28;             // inverse DFT matrix row stride in smem (words)
 constexpr int HS_B = 36;               // x+mix: words per sample row of the mode buffer
 constexpr int HS_K = 584;              // x+mix: words per kept kx of the mode buffer
 
@@ -63,6 +62,8 @@ struct FastTables {
     uint4* fwd_a;    // [group 8][mt 3][lane]       forward y DFT, rows re/im of 8 ky', cols the group
     uint4* tz_a;     // [half 2][mt 2][ks 2][lane]  inverse z DFT over a warp's 32 sites
     uint2* tzt_b;    // [half 2][kk 2][nt 3][lane]  forward z DFT over a warp's 32 sites
+    uint2* xf_b;     // [ks 8][nt 6][lane]          forward x DFT (B = fwd^T)
+    uint2* xi_b;     // [ks 3][nt 16][lane]         inverse x DFT (B = inv^T)
 };
 
 std::mutex g_fast_mu;
@@ -157,6 +158,12 @@ const FastTables* fast_tables() {
     for (int half = 0; half < 2; ++half)
         for (int kk = 0; kk < 2; ++kk)
             for (int nt = 0; nt < 3; ++nt) b_tile(tzt, 64, 8 * nt, 32 * half + 16 * kk);
+    const size_t off_xf = frags.size();
+    for (int ks = 0; ks < 8; ++ks)
+        for (int nt = 0; nt < 6; ++nt) b_tile(fwd, 128, 8 * nt, 16 * ks);
+    const size_t off_xi = frags.size();
+    for (int ks = 0; ks < 3; ++ks)
+        for (int nt = 0; nt < 16; ++nt) b_tile(inv, 48, 8 * nt, 16 * ks);
     const size_t halfs = tz.size() + tzt.size() + fwd.size() + inv.size();
     const size_t bytes = halfs * sizeof(uint16_t) + frags.size() * sizeof(uint32_t);
     unsigned char* d = nullptr;
@@ -182,6 +189,8 @@ const FastTables* fast_tables() {
     t.fwd_a = reinterpret_cast<uint4*>(fr + off_fwd);
     t.tz_a = reinterpret_cast<uint4*>(fr + off_tz);
     t.tzt_b = reinterpret_cast<uint2*>(fr + off_tzt);
+    t.xf_b = reinterpret_cast<uint2*>(fr + off_xf);
+    t.xi_b = reinterpret_cast<uint2*>(fr + off_xi);
     return &(g_fast[dev] = t);
 }
 
@@ -613,31 +622,89 @@ __global__ void __launch_bounds__(PT, 1) fno_plane_kernel(const PlaneArgs a) {
     }
 }
 
-// x DFT of one kept (ky, kz) for 16 samples, the channel mixing of its 24 modes, and
-// the inverse x DFT, in place on SY. Rows are (sample, channel), 64 x values each; a
-// row's values lie SYW words apart (SY is [b][x][(ky', kz)][c]).
+// x DFT of one kept (ky, kz) for 16 samples, the channel mixing of its 24 modes on the
+// fifth-generation tensor cores, and the inverse x DFT, in place on SY. Rows are (sample,
+// channel), 64 x values each; a row's values lie SYW words apart (SY is [b][x][(ky', kz)][c]).
+//
+// Mixing, per pair of kept kx (modes m1, m2): D[128][16] = A[128][128] x B[128][16] with
+//   A = [[W1, 0], [0, W2]] (W = the mode's 64 x 64 BF16 block, output feature x input
+//   component, columns in fragment order), B = [H1^T; H2^T] (input components x samples),
+// one tcgen05.mma chain of 8 K=16 steps, FP32 accumulation in tensor memory (16 columns
+// per pair, lane = output feature). Operands sit in shared memory in the no-swizzle
+// K-major layout: 8-row x 16-byte core matrices, K-adjacent ones 128 B apart (leading
+// byte offset), 8-row groups 1024 B apart (stride byte offset). The zero blocks of A are
+// one 8 KB zero region between W1 and W2: for the first four K steps the descriptor
+// starts at W1 (rows 64-127 then read the zeros), for the last four at the zeros (rows
+// 0-63) followed by W2. One thread issues the MMAs and commits them to an mbarrier per
+// operand buffer; the buffers alternate so that staging the next pair overlaps the
+// current pair's MMAs. Waits are bounded: a wait that gives up marks the CTA's results
+// NaN (the jump then fails its acceptance test and is rerun exactly), frees the tensor
+// memory and returns.
+constexpr int XM_TMEM_COLS = 256;       // 12 pairs x 16 columns, rounded to a power of two
+constexpr int XM_A_BYTES = 3 * 8192;    // W1 | zeros | W2
+constexpr int XM_B_BYTES = 2 * 2048;    // H1^T | H2^T
+
 struct XmixSmem {
-    uint32_t fs[48 * FWD_LD];
-    uint32_t gs[128 * INV_LD];
-    uint32_t hs[FK * HS_K];   // [kx'][sample][channel], padded strides
+    unsigned char a[2][XM_A_BYTES];     // 1024-byte aligned operand buffers first
+    unsigned char bop[2][XM_B_BYTES];
+    uint32_t hs[FK * HS_K];             // [kx'][sample][channel], padded strides
+    unsigned long long bar[2];
+    uint32_t tmem_base;
+    int failed;
 };
 
-__global__ void __launch_bounds__(256) fno_xmix_kernel(uint32_t* __restrict__ sy, const uint16_t* __restrict__ wmix,
-                                                       const uint16_t* __restrict__ fwd,
-                                                       const uint16_t* __restrict__ inv, int B) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    XmixSmem& sm = *reinterpret_cast<XmixSmem*>(smem_raw);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+    // start address >> 4 | leading byte offset 128 >> 4 | stride byte offset 1024 >> 4 | version 1
+    return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t(128 >> 4) << 16) | (uint64_t(1024 >> 4) << 32) |
+           (uint64_t(1) << 46);
+}
+// kind::f16 instruction descriptor: F32 accumulator, BF16 A and B, both K-major, N = 16, M = 128
+constexpr uint32_t kMixIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(kMixIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+
+__global__ void __launch_bounds__(256, 2) fno_xmix_kernel(uint32_t* __restrict__ sy, const uint16_t* __restrict__ wmix,
+                                                       const uint2* __restrict__ xf_b,
+                                                       const uint2* __restrict__ xi_b, int B) {
+    extern __shared__ __align__(1024) unsigned char smem_xm[];   // no static shared memory: starts at 0
+    XmixSmem& sm = *reinterpret_cast<XmixSmem*>(smem_xm);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t4 = lane & 3;
     const int p = blockIdx.x % NPK, b0 = 16 * (blockIdx.x / NPK);
     const int nb = B - b0 < 16 ? B - b0 : 16;
     uint32_t* base = sy + p * FC;
     auto at = [&](int row, int xx) { return (int64_t(b0 + row / FC) * FN + xx) * SYW + row % FC; };
-    const uint32_t* f32 = reinterpret_cast<const uint32_t*>(fwd);
-    for (int i = threadIdx.x; i < 48 * 64; i += 256) sm.fs[(i / 64) * FWD_LD + i % 64] = f32[i];
-    const uint32_t* g32 = reinterpret_cast<const uint32_t*>(inv);
-    for (int i = threadIdx.x; i < 128 * 24; i += 256) sm.gs[(i / 24) * INV_LD + i % 24] = g32[i];
-    __syncthreads();
+
+    // tensor memory (warp 0), the two commit barriers, zero regions of A
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         smem_addr(&sm.tmem_base)),
+                     "r"(XM_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(smem_addr(&sm.bar[0]), 1);
+        mbar_init(smem_addr(&sm.bar[1]), 1);
+        mbar_init_fence();
+        sm.failed = 0;
+    }
+    for (int i = tid; i < 8192 / 16; i += 256) {
+        reinterpret_cast<uint4*>(sm.a[0] + 8192)[i] = make_uint4(0u, 0u, 0u, 0u);
+        reinterpret_cast<uint4*>(sm.a[1] + 8192)[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
 
     // forward x DFT: H[row][j] = sum_k in[row][k] F[k][j]; 32 m-tiles of 16 rows, 4 per warp
     for (int i = 0; i < 4; ++i) {
@@ -649,15 +716,15 @@ __global__ void __launch_bounds__(256) fno_xmix_kernel(uint32_t* __restrict__ sy
         for (int nt = 0; nt < 6; ++nt)
 #pragma unroll
             for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
-#pragma unroll
+#pragma unroll 4
         for (int ks = 0; ks < 8; ++ks) {
             const int xx = 8 * ks + t4;
             const uint32_t A[4] = {v0 ? base[at(r0, xx)] : 0u, v1 ? base[at(r1, xx)] : 0u,
                                    v0 ? base[at(r0, xx + 4)] : 0u, v1 ? base[at(r1, xx + 4)] : 0u};
 #pragma unroll
             for (int nt = 0; nt < 6; ++nt) {
-                const uint32_t* fr = sm.fs + (nt * 8 + g) * FWD_LD + 8 * ks + t4;
-                mma(d[nt], A, fr[0], fr[4]);
+                const uint2 f = xf_b[(ks * 6 + nt) * 32 + lane];
+                mma(d[nt], A, f.x, f.y);
             }
         }
 #pragma unroll
@@ -667,45 +734,105 @@ __global__ void __launch_bounds__(256) fno_xmix_kernel(uint32_t* __restrict__ sy
             sm.hs[kx * HS_K + (r1 / FC) * HS_B + r1 % FC] = pk(d[nt][2], d[nt][3]);
         }
     }
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sm.tmem_base;
 
-    // mixing, one kept kx per pass: Z[b][n] = sum_k H[b][k] M'[k][n], k = 2 i + s, n = 2 o + s'
-    for (int i = 0; i < 3; ++i) {
-        const int kx = warp + 8 * i;
-        const uint16_t* wm = wmix + (int64_t(kx) * NPK + p) * (2 * FC) * (2 * FC);
-        uint32_t* hk = sm.hs + kx * HS_K;
-        uint32_t A[4][4];
+    // mixing on the tensor cores, one pair of kept kx per step; the weights of pair j + 1
+    // are copied while pair j is staged and multiplied
+    constexpr int NPAIR = FK / 2;
+    bool ok = true;
+    auto stage_weights = [&](int j) {   // modes (2j, 2j+1): 2 x 64 rows x 8 chunks of 16 bytes
+        if (j < NPAIR) {
+            const int u = j & 1;
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-            A[ks][0] = hk[g * HS_B + 8 * ks + t4];
-            A[ks][1] = hk[(g + 8) * HS_B + 8 * ks + t4];
-            A[ks][2] = hk[g * HS_B + 8 * ks + 4 + t4];
-            A[ks][3] = hk[(g + 8) * HS_B + 8 * ks + 4 + t4];
-        }
-        __syncwarp();
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            float z[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-                const uint2 w = wfrag(wm, 64, nt * 8 + g, ks, t4);
-                mma(z, A[ks], w.x, w.y);
+            for (int i = 0; i < 4; ++i) {
+                const int c = tid + 256 * i, half = c >> 9, rem = c & 511, n = rem >> 3, kc = rem & 7;
+                const int kx = 2 * j + half;
+                const uint16_t* src = wmix + ((int64_t(kx) * NPK + p) * 64 + n) * 64 + kc * 8;
+                cp16(sm.a[u] + half * 16384 + (n >> 3) * 1024 + kc * 128 + (n & 7) * 16, src);
             }
-            const int o = 4 * nt + t4;
-            hk[g * HS_B + o] = pk(z[0], z[1]);
-            hk[(g + 8) * HS_B + o] = pk(z[2], z[3]);
+        }
+        cp_commit();
+    };
+    stage_weights(0);
+    for (int j = 0; j < NPAIR; ++j) {
+        const int u = j & 1;
+        // buffer 1 - u was read by the MMAs of pair j - 1: wait for them before refilling it
+        if (j >= 1 && !mbar_wait_bounded(smem_addr(&sm.bar[1 - u]), uint32_t(((j - 1) >> 1) & 1))) ok = false;
+        stage_weights(j + 1);
+        // activations: H^T of both modes, 16 samples x 8 chunks of 16 bytes each, in the
+        // weights' column order (fragment order within each 16-column block)
+        {
+            const int half = tid >> 7, rem = tid & 127, bb = rem >> 3, kc = rem & 7;
+            const uint32_t* hk = sm.hs + (2 * j + half) * HS_K + bb * HS_B + 8 * (kc >> 1);
+            const uint4 v = (kc & 1) ? make_uint4(hk[2], hk[6], hk[3], hk[7]) : make_uint4(hk[0], hk[4], hk[1], hk[5]);
+            *reinterpret_cast<uint4*>(sm.bop[u] + half * 2048 + (bb >> 3) * 1024 + kc * 128 + (bb & 7) * 16) = v;
+        }
+        cp_wait1();   // pair j's weights have landed (pair j + 1's may still be in flight)
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a0 = smem_addr(sm.a[u]), bq = smem_addr(sm.bop[u]);
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const uint32_t aa = kk < 4 ? a0 + kk * 256 : a0 + 8192 + (kk - 4) * 256;
+                const uint32_t ba = kk < 4 ? bq + kk * 256 : bq + 2048 + (kk - 4) * 256;
+                umma_bf16(tmem + uint32_t(16 * j), umma_desc(aa), umma_desc(ba), kk > 0 ? 1u : 0u);
+            }
+            umma_commit(smem_addr(&sm.bar[u]));
         }
     }
+    // the last commit covers every MMA of the CTA
+    if (!mbar_wait_bounded(smem_addr(&sm.bar[(NPAIR - 1) & 1]), uint32_t(((NPAIR - 1) >> 1) & 1))) ok = false;
+    if (!ok) atomicOr(&sm.failed, 1);
+    tc_fence_after();
+    // read D back: warp w reads lanes 32 (w % 4) .. +31 (output features) of pairs
+    // 6 (w / 4) .. +5; lane 2o holds the real part of output o, lane 2o+1 the imaginary part
+    {
+        const int q4 = warp & 3, r = 32 * q4 + lane, half = r >> 6, n = r & 63;
+#pragma unroll 1
+        for (int jj = 0; jj < NPAIR / 2; ++jj) {
+            const int j = (warp >> 2) * (NPAIR / 2) + jj;
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(tmem + (uint32_t(32 * q4) << 16) + uint32_t(16 * j)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            uint32_t* hk = sm.hs + (2 * j + half) * HS_K + (n >> 1);
+#pragma unroll
+            for (int bb = 0; bb < 16; ++bb) {
+                const float re = __uint_as_float(v[bb]);
+                const float im = __shfl_down_sync(0xffffffffu, re, 1);
+                if (!(n & 1)) hk[bb * HS_B] = pk(re, im);
+            }
+        }
+    }
+    tc_fence_before();
     __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(XM_TMEM_COLS)
+                     : "memory");
+    }
+    const bool failed = sm.failed != 0;
 
-    // inverse x DFT: out[row][j] = sum_k Z[row][k] G[k][j], k = 2 kx' + s, j = 2 x + s'
-    for (int i = 0; i < 4; ++i) {
-        const int mt = warp + 8 * i;
+    // inverse x DFT: out[row][j] = sum_k Z[row][k] G[k][j], k = 2 kx' + s, j = 2 x + s'; each
+    // m-tile in two halves of 8 n-tiles (32 x values) so that fragments and sums fit in registers
+    const uint32_t nanw = 0x7FC07FC0u;
+    for (int i = 0; i < 8; ++i) {
+        const int mt = warp + 8 * (i >> 1), nh = i & 1;
         const int r0 = 16 * mt + g, r1 = r0 + 8;
         const int h0 = (r0 / FC) * HS_B + r0 % FC, h1 = (r1 / FC) * HS_B + r1 % FC;
-        float d[16][4];
+        float d[8][4];
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt)
+        for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
 #pragma unroll
@@ -714,17 +841,17 @@ __global__ void __launch_bounds__(256) fno_xmix_kernel(uint32_t* __restrict__ sy
             const uint32_t A[4] = {sm.hs[kx * HS_K + h0], sm.hs[kx * HS_K + h1], sm.hs[(kx + 4) * HS_K + h0],
                                    sm.hs[(kx + 4) * HS_K + h1]};
 #pragma unroll
-            for (int nt = 0; nt < 16; ++nt) {
-                const uint32_t* gr = sm.gs + (nt * 8 + g) * INV_LD + 8 * ks + t4;
-                mma(d[nt], A, gr[0], gr[4]);
+            for (int nt = 0; nt < 8; ++nt) {
+                const uint2 f = xi_b[(ks * 16 + 8 * nh + nt) * 32 + lane];
+                mma(d[nt], A, f.x, f.y);
             }
         }
         const bool v0 = r0 / FC < nb, v1 = r1 / FC < nb;
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            const int xx = 4 * nt + t4;
-            if (v0) base[at(r0, xx)] = pk(d[nt][0], d[nt][1]);
-            if (v1) base[at(r1, xx)] = pk(d[nt][2], d[nt][3]);
+        for (int nt = 0; nt < 8; ++nt) {
+            const int xx = 4 * (8 * nh + nt) + t4;
+            if (v0) base[at(r0, xx)] = failed ? nanw : pk(d[nt][0], d[nt][1]);
+            if (v1) base[at(r1, xx)] = failed ? nanw : pk(d[nt][2], d[nt][3]);
         }
     }
 }
@@ -871,7 +998,7 @@ int wfs_fno_fast_xmix(void* sy, const void* Wi, int32_t B, void* stream) {
     }
     const unsigned grid = unsigned(NPK) * unsigned((B + 15) / 16);
     fno_xmix_kernel<<<grid, 256, sizeof(XmixSmem), static_cast<cudaStream_t>(stream)>>>(
-        static_cast<uint32_t*>(sy), static_cast<const uint16_t*>(Wi), t->fwd, t->inv, B);
+        static_cast<uint32_t*>(sy), static_cast<const uint16_t*>(Wi), t->xf_b, t->xi_b, B);
     return st(cudaGetLastError());
 }
 

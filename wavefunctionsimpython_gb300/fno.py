@@ -599,3 +599,33 @@ def evaluate(model: FNO, data, batch, fast=False):
     nt, nn = np.concatenate(n_t), np.concatenate(n_net)
     return {"err_net": np.concatenate(e_net), "err_prior": np.concatenate(e_prior),
             "norm_err_net": np.abs(np.sqrt(nn / nt) - 1.0)}
+
+
+def _time_inference(argv=None):
+    """python -m wavefunctionsimpython_gb300.fno [batch] [reps]: CUDA-event time of the inference
+    pass (FNO.forward_fast) of a randomly initialised network on random inputs, in ms per sample."""
+    import sys
+
+    import torch
+
+    args = list(sys.argv[1:] if argv is None else argv)
+    B = int(args[0]) if args else 64
+    reps = int(args[1]) if len(args) > 1 else 5
+    cfg = FnoConfig()
+    model = FNO(cfg, seed=3)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn((B, 2, cfg.n3), dtype=torch.complex64, device="cuda", generator=g)
+    prior = torch.zeros((B, cfg.n3), dtype=torch.complex64, device="cuda")
+    model.forward_fast(x, prior, B)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(model.stream)
+    for _ in range(reps):
+        model.forward_fast(x, prior, B)
+    e1.record(model.stream)
+    torch.cuda.synchronize()
+    print(f"inference pass, batch {B}: {e0.elapsed_time(e1) / reps / B:.4f} ms per sample")
+
+
+if __name__ == "__main__":
+    _time_inference()
