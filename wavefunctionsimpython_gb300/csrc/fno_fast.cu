@@ -16,10 +16,11 @@
 //   x+mix kernel   per kept (ky, kz) and 16 samples: the 64 -> 24 kept-kx DFT, the
 //                  per-mode complex channel mixing Z = H R, and the 24 -> 64 inverse.
 //
-// Every product is mma.sync m16n8k16 (BF16 operands, FP32 accumulation); the DFT
-// matrices are BF16 constants. Per layer a site moves its h in and out (128 B) and its
-// share of the kept spectra four times (about 36 B), plus the mixing weights (56 MB per
-// layer per 16 samples).
+// The spectral mixing, the network's only dense contraction, runs on tcgen05.mma with
+// FP32 accumulators in tensor memory; the DFTs and the pointwise layers are mma.sync
+// m16n8k16 products (BF16 operands, FP32 accumulation) on BF16 constant matrices. Per
+// layer a site moves its h in and out (128 B) and its share of the kept spectra four
+// times (about 36 B), plus the mixing weights (56 MB per layer per 16 samples).
 //
 // Layouts (bf16x2 words: two channels, or the real and imaginary part of one value):
 //   H   [B][16][64^3]                   channel pairs (2j, 2j+1), as the packed layout
@@ -51,13 +52,13 @@ constexpr int NPK = FK * FM;           // kept (ky, kz) pairs
 constexpr int HS_B = 36;               // x+mix: words per sample row of the mode buffer
 constexpr int HS_K = 584;              // x+mix: words per kept kx of the mode buffer
 
-// BF16 constants of the kept-mode DFTs, per device (see fast_tables).
+// BF16 constants of the kept-mode DFTs as per-lane mma fragments (one 16- or 8-byte load
+// per fragment), per device. They are cut from four tables built on the host:
+//   tz  [64 z][32 j]   j = 2 kz + (0: cos, 1: -sin), scaled by 1/8; j >= 24 zero
+//   tzt [32 j][64 z]   the transpose of tz
+//   fwd [48 j][128 k]  forward 64 -> 24 DFT, k = 2 n + s, j = 2 k' + s'
+//   inv [128 j][48 k]  inverse 24 -> 64 DFT, k = 2 k' + s, j = 2 n + s'
 struct FastTables {
-    uint16_t* tz;    // [64 z][32 j]   j = 2 kz + (0: cos, 1: -sin) / 8, j >= 24 zero
-    uint16_t* tzt;   // [32 j][64 z]   transpose of tz
-    uint16_t* fwd;   // [48 j][128 k]  forward 64 -> 24 DFT, k = 2 n + s, j = 2 k' + s'
-    uint16_t* inv;   // [128 j][48 k]  inverse 24 -> 64 DFT, k = 2 k' + s, j = 2 n + s'
-    // the same constants as per-lane mma fragments (one 16- or 8-byte load per fragment)
     uint4* inv_a;    // [group 8][ks 3][lane]       inverse y DFT, rows re/im of the group's y
     uint4* fwd_a;    // [group 8][mt 3][lane]       forward y DFT, rows re/im of 8 ky', cols the group
     uint4* tz_a;     // [half 2][mt 2][ks 2][lane]  inverse z DFT over a warp's 32 sites
@@ -164,27 +165,13 @@ const FastTables* fast_tables() {
     const size_t off_xi = frags.size();
     for (int ks = 0; ks < 3; ++ks)
         for (int nt = 0; nt < 16; ++nt) b_tile(inv, 48, 8 * nt, 16 * ks);
-    const size_t halfs = tz.size() + tzt.size() + fwd.size() + inv.size();
-    const size_t bytes = halfs * sizeof(uint16_t) + frags.size() * sizeof(uint32_t);
-    unsigned char* d = nullptr;
-    if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
-    std::vector<unsigned char> all(bytes);
-    size_t o = 0;
-    for (auto* v : {&tz, &tzt, &fwd, &inv}) {
-        std::memcpy(all.data() + o, v->data(), v->size() * sizeof(uint16_t));
-        o += v->size() * sizeof(uint16_t);
-    }
-    std::memcpy(all.data() + o, frags.data(), frags.size() * sizeof(uint32_t));
-    if (cudaMemcpy(d, all.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
-        cudaFree(d);
+    uint32_t* fr = nullptr;
+    if (cudaMalloc(&fr, frags.size() * sizeof(uint32_t)) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(fr, frags.data(), frags.size() * sizeof(uint32_t), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(fr);
         return nullptr;
     }
     FastTables t;
-    t.tz = reinterpret_cast<uint16_t*>(d);
-    t.tzt = t.tz + tz.size();
-    t.fwd = t.tzt + tzt.size();
-    t.inv = t.fwd + fwd.size();
-    uint32_t* fr = reinterpret_cast<uint32_t*>(d + halfs * sizeof(uint16_t));   // 16-byte aligned: halfs = 16384
     t.inv_a = reinterpret_cast<uint4*>(fr + off_inv);
     t.fwd_a = reinterpret_cast<uint4*>(fr + off_fwd);
     t.tz_a = reinterpret_cast<uint4*>(fr + off_tz);
