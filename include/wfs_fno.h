@@ -145,6 +145,12 @@ int wfs_fno_fast_last(const void* h_in, const void* sy, const void* W, const flo
  * wfs_fno_pack_mix_interleaved), and the inverse x DFT. */
 int wfs_fno_fast_xmix(void* sy, const void* Wi, int32_t B, void* stream);
 
+/* Limit of wfs_fno_fast_xmix's waits for its tensor-core commits, in seconds (default 1,
+ * at most 60). A wait that gives up makes the CTA write NaN over its outputs (the jump then
+ * fails its acceptance test), after the MMAs still in flight have drained. A limit of zero
+ * makes every such wait give up at once: the test hook for that path. */
+int wfs_fno_set_wait_limit(double seconds);
+
 /* BF16 mixing weights with interleaved real and imaginary parts, in fragment order (see
  * wfs_fno_to_bf16): row 2o+s' of mode's block holds the coefficients of (Re, Im)[s] of
  * input channel i in (Re, Im)[s'] of output o, column k = 2i+s stored at the column d

@@ -47,3 +47,17 @@ def test_create_without_gpu_reports_error():
     build_ext.build()
     with pytest.raises(WfsError):
         Engine((16, 16, 16), (1.0, 1.0, 1.0))
+
+
+def test_host_only_limits_validate_arguments():
+    """The wait-limit setters touch no device: out-of-range values are refused on any machine."""
+    if shutil.which("nvcc") is None and not Path("/usr/local/cuda/bin/nvcc").exists():
+        pytest.skip("nvcc is not available to build the engine")
+    from wavefunctionsimpython_gb300 import _lib, build_ext
+
+    build_ext.build()
+    lib = _lib.load()
+    assert lib.wfs_fno_set_wait_limit(-1.0) != 0
+    assert lib.wfs_fno_set_wait_limit(61.0) != 0
+    assert lib.wfs_fno_set_wait_limit(float("nan")) != 0
+    assert lib.wfs_fno_set_wait_limit(1.0) == 0

@@ -161,20 +161,10 @@ def f32_tensor(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda().contiguous()
 
 
-@pytest.mark.parametrize("B", [3, 17])
-def test_x_dft_mixing_inverse(torch, B):
-    """A partial 16-sample chunk (3) and a full chunk plus one (17)."""
+def xmix_reference(v, R, B):
+    """Restatement of the x+mixing kernel: forward x DFT (BF16 store), mixing per mode (BF16
+    store), inverse x DFT; v is SY as float64 [b][x][ky][kz][c][2]."""
     _, F, G = tables()
-    rng = np.random.default_rng(B)
-    nm = 4 * M ** 3
-    sy, v = rand_words(torch, (B, N, K, M, C), rng)
-    R = (rng.uniform(-1, 1, (nm, C, C, 2)) / C).astype(np.float32)
-    Wi = torch.empty((nm, 2 * C, 2 * C), dtype=torch.bfloat16, device="cuda")
-    Rt = f32_tensor(torch, R)   # argument tensors stay referenced until the call returns
-    assert lib().wfs_fno_pack_mix_interleaved(ptr(Rt), ptr(Wi), C, nm, stream(torch)) == 0
-    assert lib().wfs_fno_fast_xmix(ptr(sy), ptr(Wi), B, stream(torch)) == 0
-    got = words(sy)
-    # restatement: forward x DFT (BF16 store), mixing per mode (BF16 store), inverse x DFT
     a = v.transpose(2, 3, 0, 4, 1, 5).reshape(K, M, B, C, 2 * N)          # [ky][kz][b][c][2x+s]
     H = bf16(a @ F).reshape(K, M, B, C, K, 2)                              # [ky][kz][b][i][kx][2]
     Hc = H[..., 0] + 1j * H[..., 1]
@@ -182,8 +172,46 @@ def test_x_dft_mixing_inverse(torch, B):
     mode = (np.arange(K)[:, None, None] * K + np.arange(K)[None, :, None]) * M + np.arange(M)[None, None, :]
     Z = np.einsum("yzbik,kyzio->yzbok", Hc, Rb[mode])                      # [ky][kz][b][o][kx]
     Zi = np.stack([bf16(Z.real), bf16(Z.imag)], -1).reshape(K, M, B, C, 2 * K)
-    ref = (Zi @ G).reshape(K, M, B, C, N, 2).transpose(2, 4, 0, 1, 3, 5)  # [b][x][ky][kz][c][2]
-    assert rel(got, ref) < BF16_TOL
+    return (Zi @ G).reshape(K, M, B, C, N, 2).transpose(2, 4, 0, 1, 3, 5)  # [b][x][ky][kz][c][2]
+
+
+def packed_mixing(torch, rng):
+    nm = 4 * M ** 3
+    R = (rng.uniform(-1, 1, (nm, C, C, 2)) / C).astype(np.float32)
+    Wi = torch.empty((nm, 2 * C, 2 * C), dtype=torch.bfloat16, device="cuda")
+    Rt = f32_tensor(torch, R)   # argument tensors stay referenced until the call returns
+    assert lib().wfs_fno_pack_mix_interleaved(ptr(Rt), ptr(Wi), C, nm, stream(torch)) == 0
+    return R, Wi
+
+
+@pytest.mark.parametrize("B", [3, 17])
+def test_x_dft_mixing_inverse(torch, B):
+    """A partial 16-sample chunk (3) and a full chunk plus one (17)."""
+    rng = np.random.default_rng(B)
+    sy, v = rand_words(torch, (B, N, K, M, C), rng)
+    R, Wi = packed_mixing(torch, rng)
+    assert lib().wfs_fno_fast_xmix(ptr(sy), ptr(Wi), B, stream(torch)) == 0
+    assert rel(words(sy), xmix_reference(v, R, B)) < BF16_TOL
+
+
+def test_mixing_wait_expiry_writes_nan_and_recovers(torch):
+    """With the commit-wait limit at zero every CTA gives up at once: it drains its MMAs,
+    frees its tensor memory and writes NaN over its outputs. With the limit restored the
+    same call is exact again (tensor memory was freed, the context is intact)."""
+    rng = np.random.default_rng(12)
+    B = 3
+    sy, v = rand_words(torch, (B, N, K, M, C), rng)
+    again = sy.clone()
+    R, Wi = packed_mixing(torch, rng)
+    assert lib().wfs_fno_set_wait_limit(0.0) == 0
+    try:
+        assert lib().wfs_fno_fast_xmix(ptr(sy), ptr(Wi), B, stream(torch)) == 0
+        torch.cuda.synchronize()
+    finally:
+        assert lib().wfs_fno_set_wait_limit(1.0) == 0
+    assert np.isnan(words(sy)).all()
+    assert lib().wfs_fno_fast_xmix(ptr(again), ptr(Wi), B, stream(torch)) == 0
+    assert rel(words(again), xmix_reference(v, R, B)) < BF16_TOL
 
 
 def test_lift_plane_kernel(torch):

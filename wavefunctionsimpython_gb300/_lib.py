@@ -48,7 +48,7 @@ FNO_EXPORTED = [
     "wfs_fno_spectral_weight_grad", "wfs_fno_adam", "wfs_fno_loss", "wfs_fno_sample_norms",
     "wfs_fno_make_input", "wfs_fno_scale_samples", "wfs_fno_fast_lift", "wfs_fno_fast_layer",
     "wfs_fno_fast_last", "wfs_fno_fast_xmix", "wfs_fno_pack_mix_interleaved",
-    "wfs_fno_to_bf16",
+    "wfs_fno_to_bf16", "wfs_fno_set_wait_limit",
 ]
 SCHEDULES = {"auto": 0, "axis": 1, "plane": 2}
 NPASS = 8
@@ -204,6 +204,7 @@ def load(path: str | os.PathLike | None = None):
         "wfs_fno_fast_xmix": ([vp, vp, i32, vp], C.c_int),
         "wfs_fno_pack_mix_interleaved": ([vp, vp, i32, i32, vp], C.c_int),
         "wfs_fno_to_bf16": ([vp, i32, i32, vp, i32, i32, i32, vp], C.c_int),
+        "wfs_fno_set_wait_limit": ([C.c_double], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

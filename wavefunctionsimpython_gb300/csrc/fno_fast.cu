@@ -30,6 +30,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -69,6 +70,8 @@ struct FastTables {
 
 std::mutex g_fast_mu;
 std::map<int, FastTables> g_fast;
+// limit of the mixing kernel's waits for its tensor-core commits (wfs_fno_set_wait_limit)
+std::atomic<uint64_t> g_fno_wait_ns{1000000000ull};
 
 // round-to-nearest-even float -> bfloat16 bits (host)
 uint16_t bf16_bits(double v) {
@@ -624,9 +627,10 @@ __global__ void __launch_bounds__(PT, 1) fno_plane_kernel(const PlaneArgs a) {
 // starts at W1 (rows 64-127 then read the zeros), for the last four at the zeros (rows
 // 0-63) followed by W2. One thread issues the MMAs and commits them to an mbarrier per
 // operand buffer; the buffers alternate so that staging the next pair overlaps the
-// current pair's MMAs. Waits are bounded: a wait that gives up marks the CTA's results
-// NaN (the jump then fails its acceptance test and is rerun exactly), frees the tensor
-// memory and returns.
+// current pair's MMAs. Waits are bounded (wfs_fno_set_wait_limit): a wait that gives up
+// marks the CTA's results NaN (the jump then fails its acceptance test and is rerun
+// exactly), drains the MMAs still in flight (bounded again), frees the tensor memory and
+// returns.
 constexpr int XM_TMEM_COLS = 256;       // 12 pairs x 16 columns, rounded to a power of two
 constexpr int XM_A_BYTES = 3 * 8192;    // W1 | zeros | W2
 constexpr int XM_B_BYTES = 2 * 2048;    // H1^T | H2^T
@@ -635,7 +639,7 @@ struct XmixSmem {
     unsigned char a[2][XM_A_BYTES];     // 1024-byte aligned operand buffers first
     unsigned char bop[2][XM_B_BYTES];
     uint32_t hs[FK * HS_K];             // [kx'][sample][channel], padded strides
-    unsigned long long bar[2];
+    unsigned long long bar[3];          // commits per operand buffer; [2]: all MMAs of the CTA
     uint32_t tmem_base;
     int failed;
 };
@@ -664,7 +668,7 @@ __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence:
 
 __global__ void __launch_bounds__(256, 2) fno_xmix_kernel(uint32_t* __restrict__ sy, const uint16_t* __restrict__ wmix,
                                                        const uint2* __restrict__ xf_b,
-                                                       const uint2* __restrict__ xi_b, int B) {
+                                                       const uint2* __restrict__ xi_b, int B, uint64_t wait_ns) {
     extern __shared__ __align__(1024) unsigned char smem_xm[];   // no static shared memory: starts at 0
     XmixSmem& sm = *reinterpret_cast<XmixSmem*>(smem_xm);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -685,6 +689,7 @@ __global__ void __launch_bounds__(256, 2) fno_xmix_kernel(uint32_t* __restrict__
     if (tid == 0) {
         mbar_init(smem_addr(&sm.bar[0]), 1);
         mbar_init(smem_addr(&sm.bar[1]), 1);
+        mbar_init(smem_addr(&sm.bar[2]), 1);
         mbar_init_fence();
         sm.failed = 0;
     }
@@ -747,7 +752,8 @@ __global__ void __launch_bounds__(256, 2) fno_xmix_kernel(uint32_t* __restrict__
     for (int j = 0; j < NPAIR; ++j) {
         const int u = j & 1;
         // buffer 1 - u was read by the MMAs of pair j - 1: wait for them before refilling it
-        if (j >= 1 && !mbar_wait_bounded(smem_addr(&sm.bar[1 - u]), uint32_t(((j - 1) >> 1) & 1))) ok = false;
+        if (j >= 1 && !mbar_wait_bounded(smem_addr(&sm.bar[1 - u]), uint32_t(((j - 1) >> 1) & 1), wait_ns))
+            ok = false;
         stage_weights(j + 1);
         // activations: H^T of both modes, 16 samples x 8 chunks of 16 bytes each, in the
         // weights' column order (fragment order within each 16-column block)
@@ -772,9 +778,13 @@ __global__ void __launch_bounds__(256, 2) fno_xmix_kernel(uint32_t* __restrict__
             umma_commit(smem_addr(&sm.bar[u]));
         }
     }
-    // the last commit covers every MMA of the CTA
-    if (!mbar_wait_bounded(smem_addr(&sm.bar[(NPAIR - 1) & 1]), uint32_t(((NPAIR - 1) >> 1) & 1))) ok = false;
-    if (!ok) atomicOr(&sm.failed, 1);
+    // one more commit, on its own barrier, covers every MMA of the CTA; after a wait that gave
+    // up, the MMAs still in flight are drained (bounded by the default limit) before the
+    // tensor memory is read or freed
+    if (tid == 0) umma_commit(smem_addr(&sm.bar[2]));
+    const bool done = mbar_wait_bounded(smem_addr(&sm.bar[2]), 0u, wait_ns);
+    if (!ok || !done) atomicOr(&sm.failed, 1);
+    if (!done) mbar_wait_bounded(smem_addr(&sm.bar[2]), 0u, kWaitLimitNs);
     tc_fence_after();
     // read D back: warp w reads lanes 32 (w % 4) .. +31 (output features) of pairs
     // 6 (w / 4) .. +5; lane 2o holds the real part of output o, lane 2o+1 the imaginary part
@@ -985,8 +995,15 @@ int wfs_fno_fast_xmix(void* sy, const void* Wi, int32_t B, void* stream) {
     }
     const unsigned grid = unsigned(NPK) * unsigned((B + 15) / 16);
     fno_xmix_kernel<<<grid, 256, sizeof(XmixSmem), static_cast<cudaStream_t>(stream)>>>(
-        static_cast<uint32_t*>(sy), static_cast<const uint16_t*>(Wi), t->xf_b, t->xi_b, B);
+        static_cast<uint32_t*>(sy), static_cast<const uint16_t*>(Wi), t->xf_b, t->xi_b, B,
+        g_fno_wait_ns.load(std::memory_order_relaxed));
     return st(cudaGetLastError());
+}
+
+int wfs_fno_set_wait_limit(double seconds) {
+    if (!(seconds >= 0.0) || seconds > 60.0) return WFS_ERR_ARG;
+    g_fno_wait_ns.store(uint64_t(seconds * 1e9), std::memory_order_relaxed);
+    return WFS_OK;
 }
 
 int wfs_fno_pack_mix_interleaved(const float* R, void* Wi, int32_t C, int32_t nmodes, void* stream) {
