@@ -217,8 +217,9 @@ __global__ void __launch_bounds__(kBatchThreads) batch_x_kernel(const InstDesc* 
 }
 
 // One y tile of a plane held in shared memory (ps, row stride L): the transform of
-// plane_y_tile with its loads and stores in shared memory.
-template <int L, int P, int Q, int W, int SIGN, int TP, int TQ>
+// plane_y_tile with its loads and stores in shared memory. tw is the axis table (TWL =
+// TW_ROW) or, with TW_ROW_SMEM, the plan's row block copied into shared memory.
+template <int L, int P, int Q, int W, int SIGN, int TP, int TQ, int TWL = TW_ROW>
 __device__ __forceinline__ void smem_y_tile(Cx<float>* ps, int tile, const Cx<float>* tw, float sc, Cx<float>* sm,
                                             int tid) {
     constexpr int T = cmax(P, Q);
@@ -232,7 +233,8 @@ __device__ __forceinline__ void smem_y_tile(Cx<float>* ps, int tile, const Cx<fl
         for (int i = 0; i < Q; ++i) a1[i] = active ? ps[(t + P * i) * L + col] : mk<float>(0.f, 0.f);
     }
     auto sidx = [&](int k2, int n1) { return (k2 * P + n1) * W + c; };
-    two_stage<P, Q, SIGN, TW_ROW>(a1, a2, sm, tw_rows<P, Q, TP, TQ>(tw), in_block ? t : T, sidx);
+    const Cx<float>* rows = (TWL == TW_ROW) ? tw_rows<P, Q, TP, TQ>(tw) : tw;
+    two_stage<P, Q, SIGN, TWL>(a1, a2, sm, rows, in_block ? t : T, sidx);
     if (active && t < Q) {
 #pragma unroll
         for (int k = 0; k < P; ++k) ps[(t + Q * k) * L + col] = scale(a2[k], sc);
@@ -280,7 +282,8 @@ struct PlaneSmem {
     using B = BPlan<SWAP, L>;
     static constexpr int RS = cmax(B::Q * (B::P + 1), B::P * (B::Q + 1));
     static constexpr int kTile = cmax(L * B::WS, B::WC * RS);  // transpose buffer (complex)
-    static constexpr size_t bytes = sizeof(Cx<float>) * (size_t(L) * L + kTile);
+    // the plane, the transpose buffer, the y plan's twiddle rows and the z angle table
+    static constexpr size_t bytes = sizeof(Cx<float>) * (size_t(L) * L + kTile + 2 * L);
 };
 
 // plane pass: CTA (x, j) takes yz-plane x of instance ids[j] into shared memory, applies
@@ -292,25 +295,32 @@ __global__ void __launch_bounds__(kBatchThreads) batch_plane_kernel(const InstDe
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Cx<float>* ps = reinterpret_cast<Cx<float>*>(smem_raw);
     Cx<float>* sm = ps + L * L;
+    Cx<float>* tw_y = sm + PlaneSmem<SWAP, L>::kTile;   // read by every y tile of the plane
+    Cx<float>* tw_z = tw_y + L;                         // read by every z tile
     const InstDesc in = insts[ids[blockIdx.y]];
     const int tid = threadIdx.x;
     const int64_t off = int64_t(blockIdx.x) * L * L;
     const float4* g4 = reinterpret_cast<const float4*>(in.psi + off);
     float4* s4 = reinterpret_cast<float4*>(ps);
     for (int i = tid; i < L * L / 2; i += kBatchThreads) s4[i] = __ldcs(g4 + i);
+    const Cx<float>* rows = tw_rows<B::P, B::Q, B::TP, B::TQ>(in.tw);
+    for (int i = tid; i < L; i += kBatchThreads) {
+        tw_y[i] = rows[i];
+        tw_z[i] = in.tw[i];
+    }
     __syncthreads();
     constexpr int ntile_y = (L + B::WS - 1) / B::WS;
     constexpr int ntile_z = (L + B::WC - 1) / B::WC;
     for (int tile = 0; tile < ntile_y; ++tile) {
-        smem_y_tile<L, B::P, B::Q, B::WS, +1, B::TP, B::TQ>(ps, tile, in.tw, in.sy, sm, tid);
+        smem_y_tile<L, B::P, B::Q, B::WS, +1, B::TP, B::TQ, TW_ROW_SMEM>(ps, tile, tw_y, in.sy, sm, tid);
         __syncthreads();
     }
     for (int tile = 0; tile < ntile_z; ++tile) {
-        smem_z_tile<L, B::P, B::Q, B::WC>(ps, in.ephase + off, tile, in.tw, 1.0f / float(L), sm, tid);
+        smem_z_tile<L, B::P, B::Q, B::WC>(ps, in.ephase + off, tile, tw_z, 1.0f / float(L), sm, tid);
         __syncthreads();
     }
     for (int tile = 0; tile < ntile_y; ++tile) {
-        smem_y_tile<L, B::P, B::Q, B::WS, -1, B::TP, B::TQ>(ps, tile, in.tw, in.sy, sm, tid);
+        smem_y_tile<L, B::P, B::Q, B::WS, -1, B::TP, B::TQ, TW_ROW_SMEM>(ps, tile, tw_y, in.sy, sm, tid);
         __syncthreads();
     }
     float4* d4 = reinterpret_cast<float4*>(in.psi + off);
